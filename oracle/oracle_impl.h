@@ -1,0 +1,377 @@
+/*
+ * oracle_impl.h -- CPU restatement of the reference TPR / PTPR / CR / PCR
+ * solvers, instantiated twice by oracle.c (REAL = float and REAL = double).
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker: tests, the smoke
+ * check and bench.py's CPU-baseline leg may call it; the shipped solver
+ * never does.
+ *
+ * Every update is written with the reference's own operand order (and the
+ * file is compiled with -ffp-contract=off) so that, on the same inputs, the
+ * results are bit-identical to the reference's CPU solvers built without FMA
+ * contraction.  The reference file:line each routine follows is given in its
+ * comment; paths are relative to the reference project root.
+ *
+ * Before inclusion: REAL (float|double), SFX (suffix token), ONE, EPS.
+ */
+
+#define O_CAT_(x, y) x##y
+#define O_CAT(x, y) O_CAT_(x, y)
+#define OFN(name) O_CAT(name, SFX)
+
+/* ------------------------------------------------------------------------
+ * Three-point updates used inside PCR-like sweeps.  "upper" is the update of
+ * a row with no left partner inside the range, "lower" of a row with no
+ * right partner, "mid" of a row with both.
+ *   mid   : src/ptpr.cpp:145-166 (interior loop), src/tpr.cpp:264-293,
+ *           src/cr.cpp:136-146
+ *   upper : src/ptpr.cpp:131-143, src/tpr.cpp:253-262
+ *   lower : src/ptpr.cpp:168-180, src/tpr.cpp:295-304, src/cr.cpp:148-157
+ * ---------------------------------------------------------------------- */
+static inline void OFN(upd_mid_)(const REAL *a, const REAL *c, const REAL *r,
+                                 int kl, int k, int kr, REAL *oa, REAL *oc,
+                                 REAL *orr) {
+    REAL inv = ONE / (ONE - c[kl] * a[k] - a[kr] * c[k]);
+    *oa = -inv * a[kl] * a[k];
+    *oc = -inv * c[kr] * c[k];
+    *orr = inv * (r[k] - r[kl] * a[k] - r[kr] * c[k]);
+}
+
+static inline void OFN(upd_upper_)(const REAL *a, const REAL *c,
+                                   const REAL *r, int k, int kr, REAL *oa,
+                                   REAL *oc, REAL *orr) {
+    REAL inv = ONE / (ONE - a[kr] * c[k]);
+    *oa = inv * a[k];
+    *oc = -inv * c[kr] * c[k];
+    *orr = inv * (r[k] - r[kr] * c[k]);
+}
+
+static inline void OFN(upd_lower_)(const REAL *a, const REAL *c,
+                                   const REAL *r, int kl, int k, REAL *oa,
+                                   REAL *oc, REAL *orr) {
+    REAL inv = ONE / (ONE - c[kl] * a[k]);
+    *oa = -inv * a[kl] * a[k];
+    *oc = inv * c[k];
+    *orr = inv * (r[k] - r[kl] * a[k]);
+}
+
+/* In-place diagonal normalisation performed by the 4-argument
+ * set_tridiagonal_system (src/ptpr.hpp:80-89, src/tpr.hpp:80-89,
+ * src/pcr.hpp:42-53). */
+void OFN(orc_normalize_)(int n, REAL *a, const REAL *diag, REAL *c,
+                         REAL *rhs) {
+    for (int i = 0; i < n; i++) {
+        a[i] /= diag[i];
+        c[i] /= diag[i];
+        rhs[i] /= diag[i];
+    }
+}
+
+/* ------------------------------------------------------------------------
+ * PCR (src/pcr.cpp:15-89).  Unit diagonal.  On exit rhs holds x; a and c
+ * hold the last level's couplings.  Returns the reference flop count
+ * 14*n*log2(n).
+ * ---------------------------------------------------------------------- */
+int OFN(orc_pcr_ws_)(int n, REAL *a, REAL *c, REAL *rhs, REAL *ws) {
+    int pn = orc_ilog2(n);
+    REAL *a1 = ws, *c1 = ws + n, *r1 = ws + 2 * n;
+    for (int p = 0; p < pn; p++) {
+        int s = 1 << p;
+        for (int k = 0; k < s; k++) { /* rows without a left partner */
+            int kr = k + s;
+            REAL e = ONE / (ONE - c[k] * a[kr]);
+            a1[k] = e * a[k];
+            c1[k] = -e * c[k] * c[kr];
+            r1[k] = e * (rhs[k] - c[k] * rhs[kr]);
+        }
+        for (int k = s; k < n - s; k++) { /* rows with both partners */
+            int kl = k - s, kr = k + s;
+            REAL ap = a[k], cp = c[k];
+            REAL e = ONE / (ONE - ap * c[kl] - cp * a[kr]);
+            a1[k] = -e * ap * a[kl];
+            c1[k] = -e * cp * c[kr];
+            r1[k] = e * (rhs[k] - ap * rhs[kl] - cp * rhs[kr]);
+        }
+        for (int k = n - s; k < n; k++) { /* rows without a right partner */
+            int kl = k - s;
+            REAL ap = a[k], cp = c[k];
+            REAL e = ONE / (ONE - ap * c[kl]);
+            a1[k] = -e * ap * a[kl];
+            c1[k] = e * cp;
+            r1[k] = e * (rhs[k] - ap * rhs[kl]);
+        }
+        for (int k = 0; k < n; k++) {
+            a[k] = a1[k];
+            c[k] = c1[k];
+            rhs[k] = r1[k];
+        }
+    }
+    return 14 * n * pn;
+}
+
+int OFN(orc_pcr_)(int n, REAL *a, REAL *c, REAL *rhs) {
+    REAL *ws = (REAL *)malloc(sizeof(REAL) * (size_t)(3 * n));
+    int r = OFN(orc_pcr_ws_)(n, a, c, rhs, ws);
+    free(ws);
+    return r;
+}
+
+/* ------------------------------------------------------------------------
+ * CR (src/cr.cpp:23-116): forward reduction then back substitution.  Unit
+ * diagonal (the reference's setter ignores diag, src/cr.cpp:17-21).  a, c,
+ * rhs are overwritten; x receives the solution.  Returns 17*n (0 if n==1).
+ * ---------------------------------------------------------------------- */
+int OFN(orc_cr_ws_)(int n, REAL *a, REAL *c, REAL *rhs, REAL *x,
+                    REAL *ws) {
+    if (n <= 1) {
+        x[0] = rhs[0];
+        return 0;
+    }
+    int ln = orc_ilog2(n);
+    REAL *aa = ws, *cc = ws + n, *rr = ws + 2 * n;
+    /* forward reduction, src/cr.cpp:38-82 */
+    for (int p = 0; p < ln - 1; p++) {
+        int u = 1 << p, ux = 1 << (p + 1);
+        for (int i = ux - 1; i < n - ux; i += ux)
+            OFN(upd_mid_)(a, c, rhs, i - u, i, i + u, &aa[i], &cc[i], &rr[i]);
+        OFN(upd_lower_)(a, c, rhs, n - 1 - u, n - 1, &aa[n - 1], &cc[n - 1],
+                        &rr[n - 1]);
+        for (int i = ux - 1; i < n; i += ux) {
+            a[i] = aa[i];
+            c[i] = cc[i];
+            rhs[i] = rr[i];
+        }
+    }
+    /* back substitution, src/cr.cpp:88-116 */
+    {
+        int i = n / 2 - 1, u = n / 2;
+        REAL inv_det = ONE / (ONE - c[i] * a[i + u]);
+        x[i] = (rhs[i] - c[i] * rhs[i + u]) * inv_det;
+        x[i + u] = (rhs[i + u] - rhs[i] * a[i + u]) * inv_det;
+    }
+    for (int k = ln - 2; k >= 0; k--) {
+        int u = 1 << k;
+        x[u - 1] = rhs[u - 1] - c[u - 1] * x[u - 1 + u];
+        for (int i = u - 1 + 2 * u; i < n - u; i += 2 * u)
+            x[i] = rhs[i] - a[i] * x[i - u] - c[i] * x[i + u];
+    }
+    return 17 * n;
+}
+
+int OFN(orc_cr_)(int n, REAL *a, REAL *c, REAL *rhs, REAL *x) {
+    REAL *ws = (REAL *)malloc(sizeof(REAL) * (size_t)(3 * n));
+    int r = OFN(orc_cr_ws_)(n, a, c, rhs, x, ws);
+    free(ws);
+    return r;
+}
+
+/* Intermediate stage shared by TPR and PTPR (src/ptpr.cpp:218-241,
+ * src/tpr.cpp:235-258): reduced equation j from (E_ed(j), E_st(j+1)). */
+static void OFN(tpr_inter_)(int n, int s, const REAL *a, const REAL *c,
+                            const REAL *rhs, REAL *sa, REAL *sc, REAL *sr) {
+    int m = n / s;
+    for (int i = s - 1; i < n - 1; i += s) {
+        int k = i, kr = i + 1;
+        REAL ak = a[k], akr = a[kr], ck = c[k], ckr = c[kr];
+        REAL rk = rhs[k], rkr = rhs[kr];
+        REAL inv = ONE / (ONE - akr * ck);
+        int dst = i / s;
+        sa[dst] = inv * ak;
+        sc[dst] = -inv * ckr * ck;
+        sr[dst] = inv * (rk - rkr * ck);
+    }
+    sa[m - 1] = a[n - 1];
+    sc[m - 1] = c[n - 1];
+    sr[m - 1] = rhs[n - 1];
+}
+
+/* E_st <- E_st + s1 * E_ed with the epsilon fallback
+ * (src/ptpr.cpp:185-201, src/tpr.cpp:215-228). */
+static inline void OFN(est_update_)(REAL *a, REAL *c, REAL *rhs, int st,
+                                    int ed) {
+    REAL s1;
+    if (fabs((double)c[ed]) < (double)EPS)
+        s1 = (REAL)-1.0;
+    else
+        s1 = -c[st] / c[ed];
+    a[st] += s1 * a[ed];
+    c[st] = s1;
+    rhs[st] += s1 * rhs[ed];
+}
+
+/* ------------------------------------------------------------------------
+ * PTPR (PCR-like TPR), src/ptpr.cpp:103-287.  a, c, rhs are the
+ * diag-normalised system and are overwritten as the reference does
+ * (stage 1 patches them, stage 3 restores E_st).  x[0:n] receives the
+ * solution.  Returns the reference flop count.
+ * ---------------------------------------------------------------------- */
+size_t OFN(orc_ptpr_ws_size_)(int n, int s) {
+    int m = n / s;
+    return (size_t)(3 * s + 9 * m + n + 1);
+}
+
+int OFN(orc_ptpr_ws_)(int n, int s, REAL *a, REAL *c, REAL *rhs, REAL *x,
+                      REAL *ws) {
+    int m = n / s;
+    int ls = orc_ilog2(s), lm = orc_ilog2(m);
+    REAL *aa = ws, *cc = ws + s, *rr = ws + 2 * s;
+    REAL *st2 = ws + 3 * s;
+    REAL *sa = st2, *sc = st2 + m, *sr = st2 + 2 * m;
+    REAL *ba = st2 + 3 * m, *bc = st2 + 4 * m, *br = st2 + 5 * m;
+    REAL *pws = st2 + 6 * m; /* 3m for the stage-2 PCR */
+    REAL *xs = pws + 3 * m;
+    REAL *xx = xs + 1; /* xx[-1] == 0 sentinel, src/ptpr.cpp:66-70 */
+    for (int i = 0; i < n + 1; i++) xs[i] = (REAL)0;
+
+    /* stage 1: PCR inside every slice, src/ptpr.cpp:130-213 */
+    for (int st = 0; st < n; st += s) {
+        int ed = st + s - 1;
+        for (int p = 1; p <= ls; p++) {
+            int u = 1 << (p - 1);
+            for (int i = st; i <= ed; i++) {
+                int li = i - st;
+                REAL *oa = &aa[li], *oc = &cc[li], *orr = &rr[li];
+                if (i < st + u)
+                    OFN(upd_upper_)(a, c, rhs, i, i + u, oa, oc, orr);
+                else if (i <= ed - u)
+                    OFN(upd_mid_)(a, c, rhs, i - u, i, i + u, oa, oc, orr);
+                else
+                    OFN(upd_lower_)(a, c, rhs, i - u, i, oa, oc, orr);
+            }
+            for (int i = st; i <= ed; i++) {
+                a[i] = aa[i - st];
+                c[i] = cc[i - st];
+                rhs[i] = rr[i - st];
+            }
+        }
+        int j = st / s;
+        ba[j] = a[st];
+        bc[j] = c[st];
+        br[j] = rhs[st];
+        OFN(est_update_)(a, c, rhs, st, ed);
+    }
+    /* intermediate + stage 2 (PCR on the m-system), src/ptpr.cpp:218-258 */
+    OFN(tpr_inter_)(n, s, a, c, rhs, sa, sc, sr);
+    OFN(orc_pcr_ws_)(m, sa, sc, sr, pws);
+    for (int i = s - 1; i < n; i += s) xx[i] = sr[i / s];
+
+    /* stage 3, src/ptpr.cpp:263-287 */
+    for (int st = 0; st < n; st += s) {
+        int j = st / s, ed = st + s - 1;
+        a[st] = ba[j];
+        c[st] = bc[j];
+        rhs[st] = br[j];
+        REAL key = ONE / c[ed] * (rhs[ed] - a[ed] * xx[st - 1] - xx[ed]);
+        if (c[ed] == (REAL)0) key = (REAL)0;
+        for (int i = st; i < ed; i++)
+            xx[i] = rhs[i] - a[i] * xx[st - 1] - c[i] * key;
+    }
+    for (int i = 0; i < n; i++) x[i] = xx[i];
+
+    int fp1 = m * (14 * s * ls) + 14 * m;
+    int fp2 = 9 * (m - 1) + (14 * m * lm);
+    int fp3 = m * 4 * (s - 1);
+    return fp1 + fp2 + fp3;
+}
+
+int OFN(orc_ptpr_)(int n, int s, REAL *a, REAL *c, REAL *rhs, REAL *x) {
+    REAL *ws = (REAL *)malloc(sizeof(REAL) * OFN(orc_ptpr_ws_size_)(n, s));
+    int r = OFN(orc_ptpr_ws_)(n, s, a, c, rhs, x, ws);
+    free(ws);
+    return r;
+}
+
+/* ------------------------------------------------------------------------
+ * TPR (tree partitioning), src/tpr.cpp:95-308.  Same in/out contract as
+ * orc_ptpr_.  Stage 2 is CR on the m-system.
+ * ---------------------------------------------------------------------- */
+size_t OFN(orc_tpr_ws_size_)(int n, int s) {
+    int m = n / s;
+    return (size_t)(6 * n + 7 * m);
+}
+
+int OFN(orc_tpr_ws_)(int n, int s, REAL *a, REAL *c, REAL *rhs, REAL *x,
+                     REAL *ws) {
+    int m = n / s;
+    int ls = orc_ilog2(s);
+    REAL *bka = ws, *bkc = ws + n, *bkr = ws + 2 * n;
+    REAL *aa = ws + 3 * n, *cc = ws + 4 * n, *rr = ws + 5 * n;
+    REAL *st2 = ws + 6 * n;
+    REAL *sa = st2, *sc = st2 + m, *sr = st2 + 2 * m, *sx = st2 + 3 * m;
+    REAL *cws = st2 + 4 * m; /* 3m for the stage-2 CR */
+
+    /* stage 1, src/tpr.cpp:123-230 */
+    for (int st = 0; st < n; st += s) {
+        int ed = st + s - 1;
+        for (int i = st; i <= ed; i += 2) {
+            bka[i] = a[i];
+            bkc[i] = c[i];
+            bkr[i] = rhs[i];
+        }
+        for (int p = 1; p <= ls; p++) {
+            int u = 1 << (p - 1), p2k = 1 << p;
+            OFN(upd_upper_)(a, c, rhs, st, st + u, &aa[st], &cc[st], &rr[st]);
+            for (int i = st + p2k; i <= ed - u; i += p2k)
+                OFN(upd_mid_)(a, c, rhs, i - u, i, i + u, &aa[i], &cc[i],
+                              &rr[i]);
+            for (int i = st + p2k - 1; i <= ed - u; i += p2k)
+                OFN(upd_mid_)(a, c, rhs, i - u, i, i + u, &aa[i], &cc[i],
+                              &rr[i]);
+            OFN(upd_lower_)(a, c, rhs, ed - u, ed, &aa[ed], &cc[ed], &rr[ed]);
+            for (int i = st; i <= ed; i += p2k) {
+                a[i] = aa[i];
+                c[i] = cc[i];
+                rhs[i] = rr[i];
+            }
+            for (int i = st + p2k - 1; i <= ed; i += p2k) {
+                a[i] = aa[i];
+                c[i] = cc[i];
+                rhs[i] = rr[i];
+            }
+        }
+        for (int i = st + 1; i <= ed; i += 2) {
+            bka[i] = a[i];
+            bkc[i] = c[i];
+            bkr[i] = rhs[i];
+        }
+        OFN(est_update_)(a, c, rhs, st, ed);
+    }
+    /* intermediate + stage 2 (CR on the m-system), src/tpr.cpp:235-275 */
+    OFN(tpr_inter_)(n, s, a, c, rhs, sa, sc, sr);
+    OFN(orc_cr_ws_)(m, sa, sc, sr, sx, cws);
+    for (int i = 0; i < m; i++) x[(i + 1) * s - 1] = sx[i];
+
+    /* stage 3: restore backups then log2(s) back-substitution levels,
+     * src/tpr.cpp:277-308, 381-387 */
+    for (int i = 0; i < n; i++) {
+        a[i] = bka[i];
+        c[i] = bkc[i];
+        rhs[i] = bkr[i];
+    }
+    for (int st = 0; st < n; st += s) {
+        int ed = st + s - 1;
+        for (int p = ls - 1; p >= 0; p--) {
+            int u = 1 << p;
+            int i = st + u - 1;
+            REAL xu = (i - u < 0) ? (REAL)0 : x[i - u];
+            x[i] = rhs[i] - a[i] * xu - c[i] * x[i + u];
+            for (i = st + u - 1 + 2 * u; i <= ed; i += 2 * u)
+                x[i] = rhs[i] - a[i] * x[i - u] - c[i] * x[i + u];
+        }
+    }
+    int fp1 = 28 * n - 14 * m;
+    int fp2 = 9 * (m - 1) + 17 * m;
+    int fp3 = m * 4 * (s - 1);
+    return fp1 + fp2 + fp3;
+}
+
+int OFN(orc_tpr_)(int n, int s, REAL *a, REAL *c, REAL *rhs, REAL *x) {
+    REAL *ws = (REAL *)malloc(sizeof(REAL) * OFN(orc_tpr_ws_size_)(n, s));
+    int r = OFN(orc_tpr_ws_)(n, s, a, c, rhs, x, ws);
+    free(ws);
+    return r;
+}
+
+#undef OFN
+#undef O_CAT
+#undef O_CAT_
