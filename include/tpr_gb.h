@@ -1,0 +1,203 @@
+/*
+ * tpr_gb.h -- C ABI of the GB300 tridiagonal solver library (libtprgb.so).
+ *
+ * Plain C: pointers, sizes and int status codes; no C++ or torch types.
+ * Every function returns TPRGB_OK (0) or an error code and records a
+ * message readable with tprgb_last_error() (per calling thread).  Nothing
+ * here exits or aborts the process.
+ *
+ * Systems are  a[i] x[i-1] + b[i] x[i] + c[i] x[i+1] = d[i],  i = 0..n-1,
+ * with a[0] and c[n-1] ignored (the reference requires them to be 0).
+ * Entry points taking "d_" pointers expect device memory; "stream" is a
+ * cudaStream_t passed as void* (NULL = the legacy default stream).
+ *
+ * Reference interfaces replaced (paths relative to the reference project):
+ *   classes TPR / PTPR / CR / PCR    src/tpr.hpp:44-112, src/ptpr.hpp:44-110,
+ *                                    src/cr.hpp:24-81, src/pcr.hpp:8-68
+ *   free functions TPR_CU::tpr_cu, cr_cu, PTPR_CU::ptpr_cu, pcr_cu
+ *                                    src/tpr.cuh:50-57, src/ptpr.cuh:50-57
+ * The header-only C++ layer include/tpr_gb.hpp rebuilds the class and
+ * namespace surface on top of these functions.
+ */
+#ifndef TPR_GB_H
+#define TPR_GB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define TPRGB_API __attribute__((visibility("default")))
+#else
+#define TPRGB_API
+#endif
+
+/* ---- status codes (the reference asserts / aborts / exits instead:
+ *      src/cr.hpp:72-75, src/tpr.cu:542-550, src/tpr.cu:575-579) -------- */
+#define TPRGB_OK 0
+#define TPRGB_EINVAL 1        /* bad argument (size, null pointer, kind)  */
+#define TPRGB_ENOMEM 2        /* device or pinned allocation failed       */
+#define TPRGB_EUNSUPPORTED 3  /* valid but outside this build's limits    */
+#define TPRGB_ENONFINITE 4    /* a solution or residual is NaN / Inf      */
+#define TPRGB_ETIMEOUT 5      /* a bounded device wait gave up            */
+#define TPRGB_ECUDA 6         /* a CUDA runtime call failed               */
+#define TPRGB_EBUSY 7         /* admission refused (budget or queue full) */
+#define TPRGB_ENOTFOUND 8     /* unknown ticket / handle                  */
+
+/* ---- solver families (src/lib.hpp:30-35 Solver concept) ---------------- */
+#define TPRGB_PTPR 0 /* PCR-like TPR, PCR on the reduced system */
+#define TPRGB_TPR 1  /* tree TPR, CR on the reduced system      */
+#define TPRGB_CR 2   /* cyclic reduction (unit diagonal)        */
+#define TPRGB_PCR 3  /* parallel cyclic reduction               */
+
+/* ---- element types (src/lib.hpp:8-16 `real`) --------------------------- */
+#define TPRGB_F32 0
+#define TPRGB_F64 1
+
+TPRGB_API const char *tprgb_last_error(void);
+TPRGB_API const char *tprgb_version(void);
+
+/* Reference flop count returned by solve() (src/ptpr.cpp:104-106,
+ * src/tpr.cpp:96-98, src/cr.cpp:27, src/pcr.cpp:88). */
+TPRGB_API int tprgb_flops(int kind, int n, int s, int *flops);
+
+/* =========================================================================
+ * Reference-semantics path: the reference's own algorithm (same
+ * eliminations and operand order) on the GPU, bit-identical to its CPU
+ * solvers on the same inputs.  Inputs are diag-normalised (unit diagonal).
+ * ====================================================================== */
+
+/* Scratch bytes tprgb_ref_solve_device needs for `nsys` systems (0 when the
+ * system fits one CTA's shared memory). */
+TPRGB_API int tprgb_ref_workspace_bytes(int kind, int nsys, int n, int s,
+                                        int prec, size_t *bytes);
+
+/* Solve `nsys` systems of size n (system k at element offset k*n) with the
+ * reference algorithm `kind` and slice size s (ignored for CR / PCR).
+ * d_a, d_c, d_rhs: diag-normalised inputs, left untouched; d_x: output.
+ * d_work: device scratch of tprgb_ref_workspace_bytes, or NULL if 0.
+ * Asynchronous on `stream`.  Replaces the device part of
+ * TPR_CU::tpr_cu / PTPR_CU::ptpr_cu / cr_cu / pcr_cu
+ * (src/tpr.cu:574-723, src/ptpr.cu:542-707). */
+TPRGB_API int tprgb_ref_solve_device(int kind, int nsys, int n, int s,
+                                     int prec, const void *d_a,
+                                     const void *d_c, const void *d_rhs,
+                                     void *d_x, void *d_work,
+                                     size_t work_bytes, void *stream);
+
+/* a /= diag, c /= diag, rhs /= diag elementwise on the device: the 4-arg
+ * set_tridiagonal_system (src/ptpr.hpp:80-90, src/tpr.hpp:80-89). */
+TPRGB_API int tprgb_normalize_device(int prec, int64_t neq, void *d_a,
+                                     const void *d_diag, void *d_c,
+                                     void *d_rhs, void *stream);
+
+/* ---- solver handle: the state of one TPR / PTPR / CR / PCR object ------ */
+typedef struct tprgb_solver tprgb_solver;
+
+/* Constructor (n, s) of the reference classes; s ignored for CR / PCR.
+ * Allocates the device buffers once (src/ptpr.cpp:54-96). */
+TPRGB_API int tprgb_create(int kind, int n, int s, int prec,
+                           tprgb_solver **out);
+TPRGB_API int tprgb_destroy(tprgb_solver *h);
+
+/* set_tridiagonal_system: host arrays of n elements of the handle's type,
+ * copied to the device.  diag == NULL is the 3-argument form (unit
+ * diagonal assumed); otherwise the system is normalised by diag on the
+ * device, as the 4-argument form does.  The caller's arrays are not
+ * modified (the reference divides them in place). */
+TPRGB_API int tprgb_set_system(tprgb_solver *h, const void *a,
+                               const void *diag, const void *c,
+                               const void *rhs);
+
+/* solve(): runs on the handle's stream and waits for it; *flops (may be
+ * NULL) receives the reference flop count. */
+TPRGB_API int tprgb_solve(tprgb_solver *h, int *flops);
+
+/* get_ans(x): copies the n-element solution to host memory. */
+TPRGB_API int tprgb_get_ans(tprgb_solver *h, void *x);
+
+/* Counterparts of the reference free functions (host arrays, unit
+ * diagonal, synchronous; src/tpr.cuh:50-57, src/ptpr.cuh:50-57).  Unlike
+ * the reference they keep a per-(kind, n, s) device context between calls
+ * instead of cudaMalloc/cudaFree on every call, and the double versions are
+ * implemented (the reference's are empty stubs, src/tpr.cu:726-734). */
+TPRGB_API int tprgb_tpr_cu_f32(const float *a, const float *c,
+                               const float *rhs, float *x, int n, int s);
+TPRGB_API int tprgb_ptpr_cu_f32(const float *a, const float *c,
+                                const float *rhs, float *x, int n, int s);
+TPRGB_API int tprgb_cr_cu_f32(const float *a, const float *c,
+                              const float *rhs, float *x, int n);
+TPRGB_API int tprgb_pcr_cu_f32(const float *a, const float *c,
+                               const float *rhs, float *x, int n);
+TPRGB_API int tprgb_tpr_cu_f64(const double *a, const double *c,
+                               const double *rhs, double *x, int n, int s);
+TPRGB_API int tprgb_ptpr_cu_f64(const double *a, const double *c,
+                                const double *rhs, double *x, int n, int s);
+TPRGB_API int tprgb_cr_cu_f64(const double *a, const double *c,
+                              const double *rhs, double *x, int n);
+TPRGB_API int tprgb_pcr_cu_f64(const double *a, const double *c,
+                               const double *rhs, double *x, int n);
+
+/* Releases the device contexts kept by the *_cu functions. */
+TPRGB_API int tprgb_release_cached(void);
+
+
+/* =========================================================================
+ * Batched path: many independent systems per launch, hierarchical TPR
+ * (per-thread partition sweeps, warp-shuffle PCR inside a slice, PCR of the
+ * reduced inter-slice system inside the CTA), FP32 arithmetic with optional
+ * iterative refinement.  Raw (not diag-normalised) FP32 inputs a, b, c, d.
+ * No reference counterpart for a single call: it replaces the reference's
+ * pattern of one solver object per thread looping over systems
+ * (test/examples.cpp:104-154) and one cooperative launch per system
+ * (src/ptpr.cu:542-600).
+ * ====================================================================== */
+#define TPRGB_RESID_DF 0  /* residual in compensated FP32 (~2^-48)  */
+#define TPRGB_RESID_F64 1 /* residual in native FP64                */
+
+typedef struct tprgb_batch_opts {
+    int refine_steps;    /* 0: plain FP32 solve; k: k refinement steps      */
+    int residual;        /* TPRGB_RESID_DF or TPRGB_RESID_F64               */
+    int x_f64;           /* 1: x is double[neq]; 0: x is float[neq]         */
+    int eq_per_thread;   /* 0: tuned table; otherwise 4 or 8                */
+    int threads_per_cta; /* 0: tuned table; otherwise 128, 256, 512, 1024   */
+} tprgb_batch_opts;
+
+/* Defaults: 1 refinement step, compensated residual, FP64 x, tuned tile. */
+TPRGB_API int tprgb_batch_opts_default(tprgb_batch_opts *opts);
+
+/* Solve nsys systems of size n laid out back to back (system k at element
+ * k*n of every array).  n a power of two, 16 <= n <= 8192.  Asynchronous on
+ * `stream`; allocates nothing; can be captured in a CUDA graph. */
+TPRGB_API int tprgb_batch_solve(int nsys, int n, const float *d_a,
+                                const float *d_b, const float *d_c,
+                                const float *d_d, void *d_x,
+                                const tprgb_batch_opts *opts, void *stream);
+
+/* ---- host-buffer batched solve (pinned host arrays, e.g. for callers that
+ * keep systems on the host; the counterpart of the reference wrappers'
+ * H2D -> launch -> D2H sequence, src/ptpr.cu:542-600, without per-call
+ * allocation).  The batch is cut into chunks; chunk k+1's upload overlaps
+ * chunk k's solve and chunk k-1's download on two streams. ------------- */
+typedef struct tprgb_host_ctx tprgb_host_ctx;
+
+/* Device buffers for chunks of up to chunk_eq equations (two in flight). */
+TPRGB_API int tprgb_host_ctx_create(int64_t chunk_eq, tprgb_host_ctx **out);
+TPRGB_API int tprgb_host_ctx_destroy(tprgb_host_ctx *ctx);
+
+/* Uniform batch from host arrays (system k at element k*n) into host x
+ * (double or float per opts->x_f64).  Synchronous.  Host arrays should be
+ * pinned (cudaHostAlloc / cudaHostRegister) for full copy bandwidth. */
+TPRGB_API int tprgb_batch_solve_host(tprgb_host_ctx *ctx, int nsys, int n,
+                                     const float *a, const float *b,
+                                     const float *c, const float *d, void *x,
+                                     const tprgb_batch_opts *opts);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TPR_GB_H */

@@ -1,0 +1,89 @@
+"""Batched hierarchical solver against the FP64 Thomas oracle (FP32-stored
+systems).  Tolerances: plain FP32 solve <= 1e-5 relative L2 per system;
+with refinement <= 1e-9 (the accuracy target of the refined solver)."""
+import numpy as np
+import pytest
+
+from tpr_gb300 import batch as B
+from tpr_gb300 import generate as G
+
+pytestmark = pytest.mark.gpu
+
+
+def _err(port, bt, x):
+    truth = port.batch_thomas(bt)
+    worst, per = port.batch_rel_l2(bt, x, truth)
+    return worst, per
+
+
+@pytest.mark.parametrize("n", [16, 32, 64, 128, 256, 512, 1024, 2048, 4096,
+                               8192])
+@pytest.mark.parametrize("L", [4, 8])
+def test_plain_fp32_all_sizes(cuda, port, n, L):
+    if n < 2 * L or n // L > 1024:
+        pytest.skip("tile does not cover this size")
+    nt = max(128, min(1024, n // L))
+    bt = G.uniform_batch(37, n, 1000 + n, "uneven")
+    x = B.solve_host(bt, refine_steps=0, x_f64=False, eq_per_thread=L,
+                     threads_per_cta=nt)
+    assert x.dtype == np.float32
+    worst, _ = _err(port, bt, x)
+    assert worst <= 1e-5, worst
+
+
+@pytest.mark.parametrize("n", [64, 1024, 8192])
+@pytest.mark.parametrize("resid", [B.RESID_DF, B.RESID_F64])
+def test_refined_reaches_1e9(cuda, port, n, resid):
+    bt = G.uniform_batch(29, n, 2000 + n, "uneven")
+    x = B.solve_host(bt, refine_steps=1, residual=resid)
+    assert x.dtype == np.float64
+    worst, _ = _err(port, bt, x)
+    assert worst <= 1e-9, worst
+
+
+@pytest.mark.parametrize("steps", [1, 2, 3])
+def test_weakly_dominant_refinement_steps(cuda, port, steps):
+    """Precision-stress generator (cond up to ~1e4): each step contracts
+    the error; two steps reach 1e-9."""
+    bt = G.uniform_batch(16, 4096, 77, "weak")
+    errs = []
+    for k in range(steps + 1):
+        x = B.solve_host(bt, refine_steps=k)
+        errs.append(_err(port, bt, x)[0])
+    assert all(errs[i + 1] < errs[i] or errs[i + 1] < 1e-12
+               for i in range(steps))
+    if steps >= 2:
+        assert errs[2] <= 1e-9, errs
+
+
+def test_uniform_configs_shape_sample(cuda, port):
+    """The ADI-style uniform batch shape (N=1024) on a sample of systems,
+    every tile shape giving the same accuracy."""
+    bt = G.uniform_batch(300, 1024, 5, "dominant")
+    for L, nt in ((4, 256), (4, 512), (8, 128), (8, 256), (8, 1024)):
+        x = B.solve_host(bt, refine_steps=1, eq_per_thread=L,
+                         threads_per_cta=nt)
+        worst, _ = _err(port, bt, x)
+        assert worst <= 1e-9, (L, nt, worst)
+
+
+def test_result_independent_of_batch_position(cuda):
+    """A system's solution does not depend on which CTA / slot solved it."""
+    bt = G.uniform_batch(10, 256, 9, "uneven")
+    x_all = B.solve_host(bt, refine_steps=1)
+    for k in (0, 3, 9):
+        one = G.Batch([256], *[v[k * 256:(k + 1) * 256] for v in
+                               (bt.a, bt.b, bt.c, bt.d, bt.xt)])
+        x1 = B.solve_host(one, refine_steps=1)
+        np.testing.assert_array_equal(x1, x_all[k * 256:(k + 1) * 256])
+
+
+def test_rejects_bad_arguments(cuda):
+    import tpr_gb300 as T
+    torch = cuda
+    a = torch.zeros(1000, device="cuda")
+    with pytest.raises(T.TprError):
+        B.solve(a, a, a, a, 1000)  # not a power of two
+    a = torch.zeros(1 << 15, device="cuda")
+    with pytest.raises(T.TprError):
+        B.solve(a, a, a, a, 1 << 15, eq_per_thread=8, threads_per_cta=256)

@@ -1,0 +1,162 @@
+"""Reference-semantics GPU path against the oracle: the reference's own
+outputs (tests/golden) bit for bit, the reference's known answer with its
+tolerances, and the C restatement on fresh inputs.  Calls go through the C
+ABI (tpr_gb300 is a ctypes layer over it)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import tpr_gb300 as T
+from tpr_gb300 import generate as G
+
+pytestmark = pytest.mark.gpu
+SWEEP = [4, 8, 16, 32, 64, 128, 256, 512, 1024]
+
+
+def _kat(ans, x):
+    x = np.asarray(x, np.float64)
+    assert np.all(np.abs(x - ans) <= 1e-2)
+    assert np.max((x - ans) ** 2) <= 1e-3
+
+
+def _bits_equal(x, y):
+    x = np.asarray(x)
+    y = np.asarray(y)
+    assert x.dtype == y.dtype and x.shape == y.shape
+    u = np.uint32 if x.dtype == np.float32 else np.uint64
+    np.testing.assert_array_equal(x.view(u), y.view(u))
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_fixed_system_classes(cuda, golden, ans1024, prec):
+    """test/examples.cpp:59-102 and test/cuexamples.cpp:49-83 cases."""
+    dt = np.float32 if prec == "f32" else np.float64
+    a, diag, c, rhs = [v.astype(dt) for v in G.fixed_system(1024)]
+    for cls, key in ((T.CR, "cr"), (T.PCR, "pcr")):
+        t = cls(1024, dtype=dt)
+        t.set_tridiagonal_system(a, diag, c, rhs)
+        assert t.solve() > 0
+        x = np.zeros(1024, dt)
+        assert t.get_ans(x) == 0
+        _bits_equal(x, golden[f"fixed_{key}_{prec}"])
+        _kat(ans1024, x)
+    for s in SWEEP:
+        for cls, key in ((T.PTPR, "ptpr"), (T.TPR, "tpr")):
+            t = cls(1024, s, dtype=dt)
+            t.set_tridiagonal_system(a, diag, c, rhs)
+            t.solve()
+            x = t.get_ans()
+            _bits_equal(x, golden[f"fixed_{key}_s{s}_{prec}"])
+            _kat(ans1024, x)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_fixed_system_free_functions(cuda, golden, ans1024, prec):
+    dt = np.float32 if prec == "f32" else np.float64
+    a, _, c, rhs = [v.astype(dt) for v in G.fixed_system(1024)]
+    _bits_equal(T.cr_cu(a, c, rhs, 1024, dt), golden[f"fixed_cr_{prec}"])
+    _bits_equal(T.pcr_cu(a, c, rhs, 1024, dt), golden[f"fixed_pcr_{prec}"])
+    for s in (64, 128, 256, 512, 1024):  # test/cuexamples.cpp:73-83
+        x = T.ptpr_cu(a, c, rhs, 1024, s, dt)
+        _bits_equal(x, golden[f"fixed_ptpr_s{s}_{prec}"])
+        _kat(ans1024, x)
+        x = T.tpr_cu(a, c, rhs, 1024, s, dt)
+        _bits_equal(x, golden[f"fixed_tpr_s{s}_{prec}"])
+        _kat(ans1024, x)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+@pytest.mark.parametrize("s", [64, 128, 256, 512, 1024, 2048])
+def test_plain_system_bitwise(cuda, golden, prec, s):
+    """The plain single-system workload (N=2048, seed 42), 4-arg setter on
+    the device, against the reference CPU PTPR / TPR."""
+    dt = np.float32 if prec == "f32" else np.float64
+    a, b, c, d, xt = G.one_system(2048, 42, "dominant")
+    a, b, c, d = [v.astype(dt) for v in (a, b, c, d)]
+    for cls, key in ((T.PTPR, "ptpr"), (T.TPR, "tpr")):
+        t = cls(2048, s, dtype=dt)
+        t.set_tridiagonal_system(a, b, c, d)
+        t.solve()
+        x = t.get_ans()
+        ref = golden[f"plain_{key}_s{s}_{prec}"]
+        _bits_equal(x, ref)
+        err = np.linalg.norm(x.astype(np.float64) - ref) / np.linalg.norm(ref)
+        assert err <= (1e-5 if prec == "f32" else 1e-12)
+
+
+@pytest.mark.parametrize("k", range(1, 21))
+def test_nstab_fixtures(cuda, golden, nstab, k):
+    a, diag, c, rhs = [v.astype(np.float32) for v in nstab[f"eq{k}"]]
+    for s in (16, 64, 512):
+        for cls, key in ((T.PTPR, "ptpr"), (T.TPR, "tpr")):
+            t = cls(512, s)
+            t.set_tridiagonal_system(a, diag, c, rhs)
+            t.solve()
+            _bits_equal(t.get_ans(), golden[f"nstab_eq{k}_{key}_s{s}_f32"])
+
+
+def _device_batch(torch, nsys, n, dt, seed):
+    bt = G.uniform_batch(nsys, n, seed, "uneven")
+    tdt = torch.float32 if dt == np.float32 else torch.float64
+    norm = [bt.a / bt.b, bt.c / bt.b, bt.d / bt.b]
+    if dt == np.float32:
+        norm = [(v.astype(np.float32)) for v in
+                (bt.a / bt.b, bt.c / bt.b, bt.d / bt.b)]
+    dev = [torch.from_numpy(np.ascontiguousarray(v, dt)).to("cuda", tdt)
+           for v in norm]
+    return bt, norm, dev
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+@pytest.mark.parametrize("kind,n,s", [(0, 1024, 128), (1, 1024, 128),
+                                      (0, 32768, 256), (1, 32768, 256),
+                                      (0, 65536, 1024), (1, 16384, 64),
+                                      (2, 2048, 0), (3, 2048, 0)])
+def test_device_batched_vs_port(cuda, port, prec, kind, n, s):
+    """Several systems per launch, fused and sliced shapes, against the C
+    restatement (bit for bit)."""
+    torch = cuda
+    dt = np.float32 if prec == "f32" else np.float64
+    if prec == "f64" and kind >= 2 and n > 4096:
+        pytest.skip("outside the FP64 standalone CR/PCR limit")
+    nsys = 3
+    bt, norm, (da, dc, dr) = _device_batch(torch, nsys, n, dt, 100 + n)
+    dx = torch.empty_like(da)
+    L = T.load()
+    sz = ctypes.c_size_t()
+    T.check(L.tprgb_ref_workspace_bytes(kind, nsys, n, s or n,
+                                        T.F32 if prec == "f32" else T.F64,
+                                        ctypes.byref(sz)))
+    work = torch.empty(max(1, sz.value), dtype=torch.uint8, device="cuda")
+    T.check(L.tprgb_ref_solve_device(
+        kind, nsys, n, s or n, T.F32 if prec == "f32" else T.F64,
+        da.data_ptr(), dc.data_ptr(), dr.data_ptr(), dx.data_ptr(),
+        work.data_ptr() if sz.value else None, sz.value,
+        torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    x = dx.cpu().numpy()
+    for k in range(nsys):
+        sl = slice(k * n, (k + 1) * n)
+        a, c, r = norm[0][sl], norm[1][sl], norm[2][sl]
+        if kind == 0:
+            xr, _ = port.ptpr(a, c, r, s, dt)
+        elif kind == 1:
+            xr, _ = port.tpr(a, c, r, s, dt)
+        elif kind == 2:
+            xr, _ = port.cr(a, c, r, dt)
+        else:
+            xr, _ = port.pcr(a, c, r, dt)
+        _bits_equal(x[sl], xr)
+
+
+def test_invalid_arguments_return_codes(cuda):
+    with pytest.raises(T.TprError) as e:
+        T.PTPR(1000, 8)
+    assert e.value.code == T.EINVAL
+    with pytest.raises(T.TprError) as e:
+        T.TPR(1024, 2048)
+    assert e.value.code == T.EINVAL
+    t = T.PTPR(64, 8)
+    with pytest.raises(T.TprError):
+        t.solve()  # no system set

@@ -1,0 +1,125 @@
+"""Batched solver entry points (device memory through torch, calls through
+the C ABI).
+
+    x = solve(a, b, c, d, n, refine_steps=1)        # torch CUDA tensors
+    x = solve_host(batch, refine_steps=1)           # generate.Batch -> numpy
+
+Inputs are raw FP32 systems (a[i] x[i-1] + b[i] x[i] + c[i] x[i+1] = d[i])
+laid out back to back; x is FP64 (default) or FP32.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import check, load
+
+RESID_DF, RESID_F64 = 0, 1
+
+
+class BatchOpts(C.Structure):
+    _fields_ = [("refine_steps", C.c_int), ("residual", C.c_int),
+                ("x_f64", C.c_int), ("eq_per_thread", C.c_int),
+                ("threads_per_cta", C.c_int)]
+
+
+def _declare(L):
+    vp, i = C.c_void_p, C.c_int
+    sig = {
+        "tprgb_batch_opts_default": (i, [C.POINTER(BatchOpts)]),
+        "tprgb_batch_solve": (i, [i, i, vp, vp, vp, vp, vp,
+                                  C.POINTER(BatchOpts), vp]),
+        "tprgb_host_ctx_create": (i, [C.c_int64, C.POINTER(vp)]),
+        "tprgb_host_ctx_destroy": (i, [vp]),
+        "tprgb_batch_solve_host": (i, [vp, i, i, vp, vp, vp, vp, vp,
+                                       C.POINTER(BatchOpts)]),
+    }
+    for name, (res, args) in sig.items():
+        if hasattr(L, name):
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+
+
+def opts(refine_steps: int = 1, residual: int = RESID_DF, x_f64: bool = True,
+         eq_per_thread: int = 0, threads_per_cta: int = 0) -> BatchOpts:
+    o = BatchOpts()
+    check(load().tprgb_batch_opts_default(C.byref(o)))
+    o.refine_steps = refine_steps
+    o.residual = residual
+    o.x_f64 = int(bool(x_f64))
+    o.eq_per_thread = eq_per_thread
+    o.threads_per_cta = threads_per_cta
+    return o
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("tpr_gb300.batch needs a CUDA device")
+    return torch
+
+
+def solve_into(x, a, b, c, d, n: int, o: BatchOpts | None = None,
+               stream=None) -> None:
+    """Uniform batch on the device: x, a, b, c, d are CUDA tensors; no
+    synchronisation."""
+    torch = _torch()
+    nsys = a.numel() // n
+    if stream is None:
+        stream = torch.cuda.current_stream().cuda_stream
+    check(load().tprgb_batch_solve(nsys, n, a.data_ptr(), b.data_ptr(),
+                                   c.data_ptr(), d.data_ptr(), x.data_ptr(),
+                                   C.byref(o or opts()), stream))
+
+
+def solve(a, b, c, d, n: int, refine_steps: int = 1, residual: int = RESID_DF,
+          x_f64: bool = True, **tile):
+    torch = _torch()
+    o = opts(refine_steps, residual, x_f64, **tile)
+    x = torch.empty(a.numel(), dtype=torch.float64 if x_f64 else torch.float32,
+                    device=a.device)
+    solve_into(x, a, b, c, d, n, o)
+    return x
+
+
+def solve_host(batch, refine_steps: int = 1, residual: int = RESID_DF,
+               x_f64: bool = True, **tile) -> np.ndarray:
+    """Solve a generate.Batch whose systems all have the same size."""
+    torch = _torch()
+    n = int(batch.ns[0])
+    if not np.all(batch.ns == n):
+        raise ValueError("solve_host handles uniform batches only")
+    dev = [torch.from_numpy(v).cuda() for v in (batch.a, batch.b, batch.c,
+                                                  batch.d)]
+    x = solve(*dev, n, refine_steps, residual, x_f64, **tile)
+    torch.cuda.synchronize()
+    return x.cpu().numpy()
+
+
+class HostContext:
+    """Device buffers for the host-array pipeline (tprgb_batch_solve_host)."""
+
+    def __init__(self, chunk_eq: int = 1 << 22):
+        self._h = C.c_void_p()
+        check(load().tprgb_host_ctx_create(int(chunk_eq), C.byref(self._h)))
+
+    def solve(self, nsys, n, a, b, c, d, x, o: BatchOpts | None = None):
+        """a..d, x: host arrays (numpy, ideally pinned), system k at k*n."""
+        ptr = lambda v: C.c_void_p(v.ctypes.data if isinstance(v, np.ndarray)
+                                   else v.data_ptr())
+        check(load().tprgb_batch_solve_host(self._h, nsys, n, ptr(a), ptr(b),
+                                            ptr(c), ptr(d), ptr(x),
+                                            C.byref(o or opts())))
+
+    def close(self):
+        if self._h is not None and self._h.value:
+            load().tprgb_host_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,303 @@
+// C ABI of libtprgb: status reporting, the reference-semantics path, the
+// solver handle behind the TPR / PTPR / CR / PCR class surface, and the
+// counterparts of the reference's *_cu free functions.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
+
+#include "common.cuh"
+
+namespace tprgb {
+
+static thread_local char g_err[512] = "";
+
+int fail(int code, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+    snprintf(g_err, sizeof(g_err), "%s: %s (%d)", what, cudaGetErrorString(e),
+             (int)e);
+    return e == cudaErrorMemoryAllocation ? TPRGB_ENOMEM : TPRGB_ECUDA;
+}
+
+// ref_kernels.cu
+int ref_validate(int kind, int n, int s, int prec);
+size_t ref_workspace_elems(int kind, int n, int s);
+bool ref_needs_workspace(int kind, int n, int s, int prec);
+int launch_ref(int kind, int nsys, int n, int s, int prec, const void *a,
+               const void *c, const void *r, void *x, long long stride,
+               void *work, cudaStream_t st);
+int launch_normalize(int prec, long long neq, void *a, const void *diag,
+                     void *c, void *r, cudaStream_t st);
+
+static int flops_of(int kind, int n, int s) {
+    int ln = ilog2(n);
+    switch (kind) {
+        case TPRGB_PTPR: {
+            int m = n / s, ls = ilog2(s), lm = ilog2(m);
+            return m * (14 * s * ls) + 14 * m + 9 * (m - 1) + 14 * m * lm +
+                   m * 4 * (s - 1);
+        }
+        case TPRGB_TPR: {
+            int m = n / s;
+            return 28 * n - 14 * m + 9 * (m - 1) + 17 * m + m * 4 * (s - 1);
+        }
+        case TPRGB_CR:
+            return n > 1 ? 17 * n : 0;
+        default:
+            return 14 * n * ln;
+    }
+}
+
+}  // namespace tprgb
+
+using namespace tprgb;
+
+struct tprgb_solver {
+    int kind, n, s, prec;
+    size_t esz;
+    void *d_a = nullptr, *d_c = nullptr, *d_r = nullptr, *d_diag = nullptr;
+    void *d_x = nullptr, *d_work = nullptr;
+    cudaStream_t stream = nullptr;
+    bool has_system = false;
+};
+
+extern "C" {
+
+TPRGB_API const char *tprgb_last_error(void) { return g_err; }
+
+TPRGB_API const char *tprgb_version(void) {
+    return "tpr_gb300 1.0 (sm_103a)";
+}
+
+TPRGB_API int tprgb_flops(int kind, int n, int s, int *flops) {
+    if (!flops) return fail(TPRGB_EINVAL, "flops is NULL");
+    if (kind == TPRGB_CR || kind == TPRGB_PCR) s = n;
+    if (!is_pow2(n) || !is_pow2(s) || s > n)
+        return fail(TPRGB_EINVAL, "n=%d, s=%d must be powers of two, s<=n", n, s);
+    *flops = flops_of(kind, n, s);
+    return TPRGB_OK;
+}
+
+TPRGB_API int tprgb_ref_workspace_bytes(int kind, int nsys, int n, int s,
+                                        int prec, size_t *bytes) {
+    if (!bytes) return fail(TPRGB_EINVAL, "bytes is NULL");
+    if (nsys < 0) return fail(TPRGB_EINVAL, "nsys=%d < 0", nsys);
+    int rc = ref_validate(kind, n, s, prec);
+    if (rc) return rc;
+    size_t esz = prec == TPRGB_F32 ? 4 : 8;
+    *bytes = ref_needs_workspace(kind, n, s, prec)
+                 ? ref_workspace_elems(kind, n, s) * esz * (size_t)nsys
+                 : 0;
+    return TPRGB_OK;
+}
+
+TPRGB_API int tprgb_ref_solve_device(int kind, int nsys, int n, int s,
+                                     int prec, const void *d_a,
+                                     const void *d_c, const void *d_rhs,
+                                     void *d_x, void *d_work,
+                                     size_t work_bytes, void *stream) {
+    int rc = ref_validate(kind, n, s, prec);
+    if (rc) return rc;
+    if (nsys < 0 || nsys > 65535)
+        return fail(TPRGB_EINVAL, "nsys=%d outside [0, 65535]", nsys);
+    if (nsys == 0) return TPRGB_OK;
+    if (!d_a || !d_c || !d_rhs || !d_x)
+        return fail(TPRGB_EINVAL, "null device pointer");
+    size_t need = 0;
+    tprgb_ref_workspace_bytes(kind, nsys, n, s, prec, &need);
+    if (need > 0 && (d_work == nullptr || work_bytes < need))
+        return fail(TPRGB_EINVAL,
+                    "workspace of %zu bytes needed (got %zu at %p)", need,
+                    work_bytes, d_work);
+    return launch_ref(kind, nsys, n, s, prec, d_a, d_c, d_rhs, d_x,
+                      (long long)n, d_work, (cudaStream_t)stream);
+}
+
+TPRGB_API int tprgb_normalize_device(int prec, int64_t neq, void *d_a,
+                                     const void *d_diag, void *d_c,
+                                     void *d_rhs, void *stream) {
+    if (prec != TPRGB_F32 && prec != TPRGB_F64)
+        return fail(TPRGB_EINVAL, "unknown precision %d", prec);
+    if (neq < 0) return fail(TPRGB_EINVAL, "neq < 0");
+    if (neq == 0) return TPRGB_OK;
+    if (!d_a || !d_diag || !d_c || !d_rhs)
+        return fail(TPRGB_EINVAL, "null device pointer");
+    return launch_normalize(prec, neq, d_a, d_diag, d_c, d_rhs,
+                            (cudaStream_t)stream);
+}
+
+static void free_handle(tprgb_solver *h) {
+    if (!h) return;
+    cudaFree(h->d_a);
+    cudaFree(h->d_work);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+TPRGB_API int tprgb_create(int kind, int n, int s, int prec,
+                           tprgb_solver **out) {
+    if (!out) return fail(TPRGB_EINVAL, "out is NULL");
+    *out = nullptr;
+    if (kind == TPRGB_CR || kind == TPRGB_PCR) s = n;
+    int rc = ref_validate(kind, n, s, prec);
+    if (rc) return rc;
+    tprgb_solver *h = new tprgb_solver();
+    h->kind = kind;
+    h->n = n;
+    h->s = s;
+    h->prec = prec;
+    h->esz = prec == TPRGB_F32 ? 4 : 8;
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        free_handle(h);
+        return cuda_fail(e, "cudaStreamCreateWithFlags");
+    }
+    // one allocation: a, c, rhs, diag, x
+    e = cudaMalloc(&h->d_a, 5 * (size_t)n * h->esz);
+    if (e != cudaSuccess) {
+        free_handle(h);
+        return cuda_fail(e, "cudaMalloc(solver buffers)");
+    }
+    char *p = (char *)h->d_a;
+    h->d_c = p + 1 * (size_t)n * h->esz;
+    h->d_r = p + 2 * (size_t)n * h->esz;
+    h->d_diag = p + 3 * (size_t)n * h->esz;
+    h->d_x = p + 4 * (size_t)n * h->esz;
+    if (ref_needs_workspace(kind, n, s, prec)) {
+        e = cudaMalloc(&h->d_work, ref_workspace_elems(kind, n, s) * h->esz);
+        if (e != cudaSuccess) {
+            free_handle(h);
+            return cuda_fail(e, "cudaMalloc(workspace)");
+        }
+    }
+    *out = h;
+    return TPRGB_OK;
+}
+
+TPRGB_API int tprgb_destroy(tprgb_solver *h) {
+    if (!h) return fail(TPRGB_EINVAL, "handle is NULL");
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_handle(h);
+    return TPRGB_OK;
+}
+
+TPRGB_API int tprgb_set_system(tprgb_solver *h, const void *a,
+                               const void *diag, const void *c,
+                               const void *rhs) {
+    if (!h) return fail(TPRGB_EINVAL, "handle is NULL");
+    if (!a || !c || !rhs) return fail(TPRGB_EINVAL, "null host array");
+    size_t bytes = (size_t)h->n * h->esz;
+    TPRGB_CUDA(cudaMemcpyAsync(h->d_a, a, bytes, cudaMemcpyHostToDevice, h->stream));
+    TPRGB_CUDA(cudaMemcpyAsync(h->d_c, c, bytes, cudaMemcpyHostToDevice, h->stream));
+    TPRGB_CUDA(cudaMemcpyAsync(h->d_r, rhs, bytes, cudaMemcpyHostToDevice, h->stream));
+    // CR ignores diag as the reference's setter does (src/cr.cpp:17-21)
+    if (diag && h->kind != TPRGB_CR) {
+        TPRGB_CUDA(cudaMemcpyAsync(h->d_diag, diag, bytes,
+                                   cudaMemcpyHostToDevice, h->stream));
+        int rc = launch_normalize(h->prec, h->n, h->d_a, h->d_diag, h->d_c,
+                                  h->d_r, h->stream);
+        if (rc) return rc;
+    }
+    // pageable sources: make the copies complete before the caller may
+    // reuse its arrays
+    TPRGB_CUDA(cudaStreamSynchronize(h->stream));
+    h->has_system = true;
+    return TPRGB_OK;
+}
+
+TPRGB_API int tprgb_solve(tprgb_solver *h, int *flops) {
+    if (!h) return fail(TPRGB_EINVAL, "handle is NULL");
+    if (!h->has_system)
+        return fail(TPRGB_EINVAL, "set_tridiagonal_system was not called");
+    int rc = launch_ref(h->kind, 1, h->n, h->s, h->prec, h->d_a, h->d_c,
+                        h->d_r, h->d_x, h->n, h->d_work, h->stream);
+    if (rc) return rc;
+    TPRGB_CUDA(cudaStreamSynchronize(h->stream));
+    if (flops) *flops = flops_of(h->kind, h->n, h->s);
+    return TPRGB_OK;
+}
+
+TPRGB_API int tprgb_get_ans(tprgb_solver *h, void *x) {
+    if (!h) return fail(TPRGB_EINVAL, "handle is NULL");
+    if (!x) return fail(TPRGB_EINVAL, "x is NULL");
+    TPRGB_CUDA(cudaMemcpyAsync(x, h->d_x, (size_t)h->n * h->esz,
+                               cudaMemcpyDeviceToHost, h->stream));
+    TPRGB_CUDA(cudaStreamSynchronize(h->stream));
+    return TPRGB_OK;
+}
+
+// ---- *_cu counterparts ----------------------------------------------------
+static std::mutex g_cache_mu;
+static std::map<std::tuple<int, int, int, int>, tprgb_solver *> g_cache;
+
+static int cu_solve(int kind, int prec, const void *a, const void *c,
+                    const void *rhs, void *x, int n, int s) {
+    if (!a || !c || !rhs || !x) return fail(TPRGB_EINVAL, "null host array");
+    if (kind == TPRGB_CR || kind == TPRGB_PCR) s = n;
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    auto key = std::make_tuple(kind, prec, n, s);
+    tprgb_solver *h;
+    auto it = g_cache.find(key);
+    if (it == g_cache.end()) {
+        int rc = tprgb_create(kind, n, s, prec, &h);
+        if (rc) return rc;
+        g_cache[key] = h;
+    } else {
+        h = it->second;
+    }
+    int rc = tprgb_set_system(h, a, nullptr, c, rhs);
+    if (!rc) rc = tprgb_solve(h, nullptr);
+    if (!rc) rc = tprgb_get_ans(h, x);
+    return rc;
+}
+
+TPRGB_API int tprgb_tpr_cu_f32(const float *a, const float *c,
+                               const float *rhs, float *x, int n, int s) {
+    return cu_solve(TPRGB_TPR, TPRGB_F32, a, c, rhs, x, n, s);
+}
+TPRGB_API int tprgb_ptpr_cu_f32(const float *a, const float *c,
+                                const float *rhs, float *x, int n, int s) {
+    return cu_solve(TPRGB_PTPR, TPRGB_F32, a, c, rhs, x, n, s);
+}
+TPRGB_API int tprgb_cr_cu_f32(const float *a, const float *c,
+                              const float *rhs, float *x, int n) {
+    return cu_solve(TPRGB_CR, TPRGB_F32, a, c, rhs, x, n, n);
+}
+TPRGB_API int tprgb_pcr_cu_f32(const float *a, const float *c,
+                               const float *rhs, float *x, int n) {
+    return cu_solve(TPRGB_PCR, TPRGB_F32, a, c, rhs, x, n, n);
+}
+TPRGB_API int tprgb_tpr_cu_f64(const double *a, const double *c,
+                               const double *rhs, double *x, int n, int s) {
+    return cu_solve(TPRGB_TPR, TPRGB_F64, a, c, rhs, x, n, s);
+}
+TPRGB_API int tprgb_ptpr_cu_f64(const double *a, const double *c,
+                                const double *rhs, double *x, int n, int s) {
+    return cu_solve(TPRGB_PTPR, TPRGB_F64, a, c, rhs, x, n, s);
+}
+TPRGB_API int tprgb_cr_cu_f64(const double *a, const double *c,
+                              const double *rhs, double *x, int n) {
+    return cu_solve(TPRGB_CR, TPRGB_F64, a, c, rhs, x, n, n);
+}
+TPRGB_API int tprgb_pcr_cu_f64(const double *a, const double *c,
+                               const double *rhs, double *x, int n) {
+    return cu_solve(TPRGB_PCR, TPRGB_F64, a, c, rhs, x, n, n);
+}
+
+TPRGB_API int tprgb_release_cached(void) {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    for (auto &kv : g_cache) tprgb_destroy(kv.second);
+    g_cache.clear();
+    return TPRGB_OK;
+}
+
+}  // extern "C"

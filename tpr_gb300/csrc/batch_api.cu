@@ -1,0 +1,155 @@
+// C ABI of the batched solver: options, tile selection, uniform batches.
+#include <algorithm>
+
+#include "batch.cuh"
+
+namespace tprgb {
+
+// Default tile per system size (equations per thread, threads per CTA),
+// replaced at run time by the autotuner's table when one is loaded.
+TileConfig default_tile(int n) {
+    if (n <= 64) return TileConfig{4, 256};
+    if (n <= 1024) return TileConfig{8, 256};
+    if (n <= 2048) return TileConfig{8, 256};
+    if (n <= 4096) return TileConfig{8, 512};
+    return TileConfig{8, 1024};
+}
+
+}  // namespace tprgb
+
+using namespace tprgb;
+
+extern "C" {
+
+TPRGB_API int tprgb_batch_opts_default(tprgb_batch_opts *o) {
+    if (!o) return fail(TPRGB_EINVAL, "opts is NULL");
+    o->refine_steps = 1;
+    o->residual = TPRGB_RESID_DF;
+    o->x_f64 = 1;
+    o->eq_per_thread = 0;
+    o->threads_per_cta = 0;
+    return TPRGB_OK;
+}
+
+TPRGB_API int tprgb_batch_solve(int nsys, int n, const float *d_a,
+                                const float *d_b, const float *d_c,
+                                const float *d_d, void *d_x,
+                                const tprgb_batch_opts *opts, void *stream) {
+    tprgb_batch_opts o;
+    if (opts)
+        o = *opts;
+    else
+        tprgb_batch_opts_default(&o);
+    if (nsys < 0) return fail(TPRGB_EINVAL, "nsys=%d < 0", nsys);
+    if (o.refine_steps < 0 || o.refine_steps > 8)
+        return fail(TPRGB_EINVAL, "refine_steps=%d outside [0, 8]", o.refine_steps);
+    if (o.residual != TPRGB_RESID_DF && o.residual != TPRGB_RESID_F64)
+        return fail(TPRGB_EINVAL, "unknown residual mode %d", o.residual);
+    if (nsys > 0 && (!d_a || !d_b || !d_c || !d_d || !d_x))
+        return fail(TPRGB_EINVAL, "null device pointer");
+    for (const void *p : {(const void *)d_a, (const void *)d_b,
+                          (const void *)d_c, (const void *)d_d,
+                          (const void *)d_x})
+        if (((uintptr_t)p & 15) != 0)
+            return fail(TPRGB_EINVAL, "device arrays must be 16-byte aligned");
+    TileConfig cfg = default_tile(n);
+    if (o.eq_per_thread) cfg.L = o.eq_per_thread;
+    if (o.threads_per_cta) cfg.nt = o.threads_per_cta;
+    BatchArgs A{d_a, d_b, d_c, d_d, d_x, nsys, n, o.refine_steps, o.residual,
+                o.x_f64};
+    return launch_batch_uniform(A, cfg, (cudaStream_t)stream);
+}
+
+}  // extern "C"
+
+// ---- host-buffer pipeline -------------------------------------------------
+struct tprgb_host_ctx {
+    int64_t chunk_eq = 0;
+    cudaStream_t st[2] = {nullptr, nullptr};
+    cudaEvent_t up[2] = {nullptr, nullptr};
+    float *d_in[2] = {nullptr, nullptr};  // a, b, c, d of one chunk
+    void *d_x[2] = {nullptr, nullptr};    // x of one chunk (8 B / eq)
+};
+
+static void host_ctx_free(tprgb_host_ctx *h) {
+    for (int i = 0; i < 2; i++) {
+        if (h->st[i]) cudaStreamDestroy(h->st[i]);
+        if (h->up[i]) cudaEventDestroy(h->up[i]);
+        cudaFree(h->d_in[i]);
+        cudaFree(h->d_x[i]);
+    }
+    delete h;
+}
+
+extern "C" {
+
+TPRGB_API int tprgb_host_ctx_create(int64_t chunk_eq, tprgb_host_ctx **out) {
+    if (!out) return fail(TPRGB_EINVAL, "out is NULL");
+    *out = nullptr;
+    if (chunk_eq <= 0 || (chunk_eq & 3))
+        return fail(TPRGB_EINVAL, "chunk_eq=%lld must be a positive multiple of 4",
+                    (long long)chunk_eq);
+    tprgb_host_ctx *h = new tprgb_host_ctx();
+    h->chunk_eq = chunk_eq;
+    for (int i = 0; i < 2; i++) {
+        cudaError_t e = cudaStreamCreateWithFlags(&h->st[i], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->up[i], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaMalloc(&h->d_in[i], 4 * sizeof(float) * (size_t)chunk_eq);
+        if (e == cudaSuccess) e = cudaMalloc(&h->d_x[i], sizeof(double) * (size_t)chunk_eq);
+        if (e != cudaSuccess) {
+            host_ctx_free(h);
+            return cuda_fail(e, "tprgb_host_ctx_create");
+        }
+    }
+    *out = h;
+    return TPRGB_OK;
+}
+
+TPRGB_API int tprgb_host_ctx_destroy(tprgb_host_ctx *h) {
+    if (!h) return fail(TPRGB_EINVAL, "ctx is NULL");
+    for (int i = 0; i < 2; i++) cudaStreamSynchronize(h->st[i]);
+    host_ctx_free(h);
+    return TPRGB_OK;
+}
+
+TPRGB_API int tprgb_batch_solve_host(tprgb_host_ctx *h, int nsys, int n,
+                                     const float *a, const float *b,
+                                     const float *c, const float *d, void *x,
+                                     const tprgb_batch_opts *opts) {
+    if (!h) return fail(TPRGB_EINVAL, "ctx is NULL");
+    if (nsys < 0 || n <= 0) return fail(TPRGB_EINVAL, "bad nsys/n");
+    if (nsys == 0) return TPRGB_OK;
+    if (!a || !b || !c || !d || !x) return fail(TPRGB_EINVAL, "null host array");
+    tprgb_batch_opts o;
+    if (opts)
+        o = *opts;
+    else
+        tprgb_batch_opts_default(&o);
+    const int64_t per = h->chunk_eq / n;  // systems per chunk
+    if (per < 1)
+        return fail(TPRGB_EINVAL, "chunk of %lld equations < one system (n=%d)",
+                    (long long)h->chunk_eq, n);
+    const size_t xs = o.x_f64 ? sizeof(double) : sizeof(float);
+    int k = 0;
+    for (int64_t s0 = 0; s0 < nsys; s0 += per, k ^= 1) {
+        const int64_t ns = std::min<int64_t>(per, nsys - s0);
+        const int64_t off = s0 * n, neq = ns * n;
+        cudaStream_t st = h->st[k];
+        float *da = h->d_in[k], *db = da + h->chunk_eq, *dc = db + h->chunk_eq,
+              *dd = dc + h->chunk_eq;
+        const size_t bytes = sizeof(float) * (size_t)neq;
+        TPRGB_CUDA(cudaMemcpyAsync(da, a + off, bytes, cudaMemcpyHostToDevice, st));
+        TPRGB_CUDA(cudaMemcpyAsync(db, b + off, bytes, cudaMemcpyHostToDevice, st));
+        TPRGB_CUDA(cudaMemcpyAsync(dc, c + off, bytes, cudaMemcpyHostToDevice, st));
+        TPRGB_CUDA(cudaMemcpyAsync(dd, d + off, bytes, cudaMemcpyHostToDevice, st));
+        int rc = tprgb_batch_solve((int)ns, n, da, db, dc, dd, h->d_x[k], &o, st);
+        if (rc) return rc;
+        TPRGB_CUDA(cudaMemcpyAsync((char *)x + off * xs, h->d_x[k], xs * (size_t)neq,
+                                   cudaMemcpyDeviceToHost, st));
+    }
+    TPRGB_CUDA(cudaStreamSynchronize(h->st[0]));
+    TPRGB_CUDA(cudaStreamSynchronize(h->st[1]));
+    return TPRGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,700 @@
+// Reference-semantics TPR / PTPR / CR / PCR kernels.
+//
+// These reproduce the reference solvers' arithmetic step for step -- the
+// same eliminations, the same operand order, IEEE division, and this
+// translation unit is compiled with -fmad=false -- so on the same inputs
+// they return the same bits as the reference's CPU classes
+// (src/ptpr.cpp:103-287, src/tpr.cpp:95-308, src/cr.cpp:23-116,
+// src/pcr.cpp:15-89).  They are the plain single-system path (one system per
+// CTA, any number of systems per launch) and the FP64 path.
+//
+// Two shapes:
+//  * fused: one CTA holds a whole system in shared memory and runs stage 1,
+//    the intermediate stage, stage 2 and stage 3 with CTA barriers only.
+//    The reference instead needs one CTA per slice and a cooperative grid
+//    sync between stages (src/ptpr.cu:48-150), which caps it at n <= s^2.
+//  * sliced (systems too large for one CTA's shared memory): stage 1 per
+//    slice CTA -> global workspace, stage 2 in one CTA per system, stage 3
+//    per slice CTA.  Three launches on one stream, no grid sync.
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace tprgb {
+namespace refk {
+
+constexpr int kThreads = 1024;
+constexpr int kEpt = 8;  // max elements per thread in a CTA sweep
+
+// ---- three-point updates (operand order of the CPU reference) ----------
+// mid: src/ptpr.cpp:145-166, upper: :131-143, lower: :168-180
+template <typename T>
+__device__ __forceinline__ void upd_mid(const T *a, const T *c, const T *r,
+                                        int kl, int k, int kr, T &oa, T &oc,
+                                        T &orr) {
+    T inv = T(1) / (T(1) - c[kl] * a[k] - a[kr] * c[k]);
+    oa = -inv * a[kl] * a[k];
+    oc = -inv * c[kr] * c[k];
+    orr = inv * (r[k] - r[kl] * a[k] - r[kr] * c[k]);
+}
+template <typename T>
+__device__ __forceinline__ void upd_upper(const T *a, const T *c, const T *r,
+                                          int k, int kr, T &oa, T &oc,
+                                          T &orr) {
+    T inv = T(1) / (T(1) - a[kr] * c[k]);
+    oa = inv * a[k];
+    oc = -inv * c[kr] * c[k];
+    orr = inv * (r[k] - r[kr] * c[k]);
+}
+template <typename T>
+__device__ __forceinline__ void upd_lower(const T *a, const T *c, const T *r,
+                                          int kl, int k, T &oa, T &oc,
+                                          T &orr) {
+    T inv = T(1) / (T(1) - c[kl] * a[k]);
+    oa = -inv * a[kl] * a[k];
+    oc = inv * c[k];
+    orr = inv * (r[k] - r[kl] * a[k]);
+}
+
+// PTPR stage 1 on rows [0, n) of shared arrays holding whole slices of size
+// s: log2(s) PCR steps with slice-local boundaries (src/ptpr.cpp:130-190).
+template <typename T>
+__device__ void ptpr_stage1(T *a, T *c, T *r, int n, int s) {
+    const int ls = ilog2(s);
+    for (int p = 1; p <= ls; p++) {
+        const int u = 1 << (p - 1);
+        T na[kEpt], nc[kEpt], nr[kEpt];
+#pragma unroll
+        for (int e = 0; e < kEpt; e++) {
+            int i = threadIdx.x + e * blockDim.x;
+            if (i < n) {
+                int li = i & (s - 1);
+                if (li < u)
+                    upd_upper(a, c, r, i, i + u, na[e], nc[e], nr[e]);
+                else if (li <= s - 1 - u)
+                    upd_mid(a, c, r, i - u, i, i + u, na[e], nc[e], nr[e]);
+                else
+                    upd_lower(a, c, r, i - u, i, na[e], nc[e], nr[e]);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < kEpt; e++) {
+            int i = threadIdx.x + e * blockDim.x;
+            if (i < n) {
+                a[i] = na[e];
+                c[i] = nc[e];
+                r[i] = nr[e];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// TPR stage 1 tree levels (src/tpr.cpp:246-317): at level p only rows with
+// li % 2^p == 0 or (li+1) % 2^p == 0 are updated.
+template <typename T>
+__device__ void tpr_stage1(T *a, T *c, T *r, int n, int s) {
+    const int ls = ilog2(s);
+    for (int p = 1; p <= ls; p++) {
+        const int u = 1 << (p - 1), p2k = 1 << p;
+        T na[kEpt], nc[kEpt], nr[kEpt];
+        bool sel[kEpt];
+#pragma unroll
+        for (int e = 0; e < kEpt; e++) {
+            int i = threadIdx.x + e * blockDim.x;
+            sel[e] = false;
+            if (i < n) {
+                int li = i & (s - 1);
+                sel[e] = ((li & (p2k - 1)) == 0) || (((li + 1) & (p2k - 1)) == 0);
+                if (sel[e]) {
+                    if (li == 0)
+                        upd_upper(a, c, r, i, i + u, na[e], nc[e], nr[e]);
+                    else if (li == s - 1)
+                        upd_lower(a, c, r, i - u, i, na[e], nc[e], nr[e]);
+                    else
+                        upd_mid(a, c, r, i - u, i, i + u, na[e], nc[e], nr[e]);
+                }
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < kEpt; e++) {
+            int i = threadIdx.x + e * blockDim.x;
+            if (sel[e]) {
+                a[i] = na[e];
+                c[i] = nc[e];
+                r[i] = nr[e];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// E_st <- E_st + s1 E_ed (src/ptpr.cpp:192-201, src/tpr.cpp:327-340).
+template <typename T>
+__device__ __forceinline__ void est_update(T *a, T *c, T *r, int st, int ed) {
+    T s1;
+    if (fabs(c[ed]) < Eps<T>::value)
+        s1 = T(-1.0);
+    else
+        s1 = -c[st] / c[ed];
+    a[st] += s1 * a[ed];
+    c[st] = s1;
+    r[st] += s1 * r[ed];
+}
+
+// Reduced equation j from rows ed_j = j*s + s - 1 and ed_j + 1
+// (src/ptpr.cpp:218-241).  row(k) returns (a, c, r) of row k.
+template <typename T>
+__device__ __forceinline__ void inter_eq(T ak, T ck, T rk, T akr, T ckr,
+                                         T rkr, T &sa, T &sc, T &sr) {
+    T inv = T(1) / (T(1) - akr * ck);
+    sa = inv * ak;
+    sc = -inv * ckr * ck;
+    sr = inv * (rk - rkr * ck);
+}
+
+// PCR on m rows in shared memory (src/pcr.cpp:15-89); rhs holds x on exit.
+template <typename T>
+__device__ void cta_pcr(T *a, T *c, T *r, int m) {
+    const int pn = ilog2(m);
+    for (int p = 0; p < pn; p++) {
+        const int s = 1 << p;
+        T na[kEpt], nc[kEpt], nr[kEpt];
+#pragma unroll
+        for (int e = 0; e < kEpt; e++) {
+            int k = threadIdx.x + e * blockDim.x;
+            if (k < m) {
+                if (k < s) {
+                    int kr = k + s;
+                    T ee = T(1) / (T(1) - c[k] * a[kr]);
+                    na[e] = ee * a[k];
+                    nc[e] = -ee * c[k] * c[kr];
+                    nr[e] = ee * (r[k] - c[k] * r[kr]);
+                } else if (k < m - s) {
+                    int kl = k - s, kr = k + s;
+                    T ap = a[k], cp = c[k];
+                    T ee = T(1) / (T(1) - ap * c[kl] - cp * a[kr]);
+                    na[e] = -ee * ap * a[kl];
+                    nc[e] = -ee * cp * c[kr];
+                    nr[e] = ee * (r[k] - ap * r[kl] - cp * r[kr]);
+                } else {
+                    int kl = k - s;
+                    T ap = a[k], cp = c[k];
+                    T ee = T(1) / (T(1) - ap * c[kl]);
+                    na[e] = -ee * ap * a[kl];
+                    nc[e] = ee * cp;
+                    nr[e] = ee * (r[k] - ap * r[kl]);
+                }
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < kEpt; e++) {
+            int k = threadIdx.x + e * blockDim.x;
+            if (k < m) {
+                a[k] = na[e];
+                c[k] = nc[e];
+                r[k] = nr[e];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// CR on m rows in shared memory (src/cr.cpp:23-116); solution into x.
+template <typename T>
+__device__ void cta_cr(T *a, T *c, T *r, T *x, int m) {
+    if (m <= 1) {
+        if (threadIdx.x == 0) x[0] = r[0];
+        __syncthreads();
+        return;
+    }
+    const int ln = ilog2(m);
+    for (int p = 0; p < ln - 1; p++) {
+        const int u = 1 << p, ux = 1 << (p + 1);
+        const int rows = m / ux;  // rows ux-1 + ux*j, j < rows; last is m-1
+        T na[kEpt], nc[kEpt], nr[kEpt];
+#pragma unroll
+        for (int e = 0; e < kEpt; e++) {
+            int j = threadIdx.x + e * blockDim.x;
+            if (j < rows) {
+                int i = ux - 1 + ux * j;
+                if (i < m - ux)
+                    upd_mid(a, c, r, i - u, i, i + u, na[e], nc[e], nr[e]);
+                else
+                    upd_lower(a, c, r, i - u, i, na[e], nc[e], nr[e]);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < kEpt; e++) {
+            int j = threadIdx.x + e * blockDim.x;
+            if (j < rows) {
+                int i = ux - 1 + ux * j;
+                a[i] = na[e];
+                c[i] = nc[e];
+                r[i] = nr[e];
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        int i = m / 2 - 1, u = m / 2;
+        T inv_det = T(1) / (T(1) - c[i] * a[i + u]);
+        x[i] = (r[i] - c[i] * r[i + u]) * inv_det;
+        x[i + u] = (r[i + u] - r[i] * a[i + u]) * inv_det;
+    }
+    __syncthreads();
+    for (int k = ln - 2; k >= 0; k--) {
+        const int u = 1 << k;
+        const int rows = m / (2 * u);  // rows u-1 + 2u*j
+        for (int j = threadIdx.x; j < rows; j += blockDim.x) {
+            int i = u - 1 + 2 * u * j;
+            if (j == 0)
+                x[i] = r[i] - c[i] * x[i + u];
+            else if (i < m - u)
+                x[i] = r[i] - a[i] * x[i - u] - c[i] * x[i + u];
+        }
+        __syncthreads();
+    }
+}
+
+// Shared-memory footprint of the fused kernel, in elements of T.
+__host__ __device__ inline long long fused_elems(int n, int s) {
+    long long m = n / s;
+    return 4LL * n + 2 + 7 * m;
+}
+
+// One CTA per system: the whole TPR / PTPR solve in shared memory.
+// Inputs are diag-normalised (unit diagonal) and left untouched.
+template <typename T, int KIND>
+__global__ void __launch_bounds__(kThreads)
+fused_tpr(const T *__restrict__ ga, const T *__restrict__ gc,
+          const T *__restrict__ gr, T *__restrict__ gx, int n, int s,
+          long long stride) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sm = reinterpret_cast<T *>(smem_raw);
+    const int m = n / s;
+    T *a = sm, *c = sm + n, *r = sm + 2 * n;
+    T *xs = sm + 3 * n;  // xs[0] is the x[-1] = 0 sentinel
+    T *x = xs + 1;
+    T *sa = xs + n + 1, *sc = sa + m, *sr = sc + m, *sx = sr + m;
+    T *ba = sx + m, *bc = ba + m, *br = bc + m;
+    const long long base = (long long)blockIdx.x * stride;
+    ga += base;
+    gc += base;
+    gr += base;
+    gx += base;
+
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        a[i] = ga[i];
+        c[i] = gc[i];
+        r[i] = gr[i];
+    }
+    if (threadIdx.x == 0) xs[0] = T(0);
+    __syncthreads();
+
+    if (KIND == TPRGB_PTPR)
+        ptpr_stage1(a, c, r, n, s);
+    else
+        tpr_stage1(a, c, r, n, s);
+
+    for (int j = threadIdx.x; j < m; j += blockDim.x) {
+        int st = j * s, ed = st + s - 1;
+        if (KIND == TPRGB_PTPR) {  // backup E_st for stage 3
+            ba[j] = a[st];
+            bc[j] = c[st];
+            br[j] = r[st];
+        }
+        est_update(a, c, r, st, ed);
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < m; j += blockDim.x) {
+        int k = j * s + s - 1;
+        if (j < m - 1)
+            inter_eq(a[k], c[k], r[k], a[k + 1], c[k + 1], r[k + 1], sa[j],
+                     sc[j], sr[j]);
+        else {
+            sa[j] = a[n - 1];
+            sc[j] = c[n - 1];
+            sr[j] = r[n - 1];
+        }
+    }
+    __syncthreads();
+
+    if (KIND == TPRGB_PTPR) {
+        cta_pcr(sa, sc, sr, m);  // src/ptpr.cpp:246-258
+        for (int j = threadIdx.x; j < m; j += blockDim.x)
+            x[j * s + s - 1] = sr[j];
+        for (int j = threadIdx.x; j < m; j += blockDim.x) {
+            int st = j * s;  // restore E_st, src/ptpr.cpp:266-271
+            a[st] = ba[j];
+            c[st] = bc[j];
+            r[st] = br[j];
+        }
+        __syncthreads();
+        // stage 3, src/ptpr.cpp:263-287
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            int st = i & ~(s - 1), ed = st + s - 1;
+            if (i == ed) continue;
+            T key = T(1) / c[ed] * (r[ed] - a[ed] * x[st - 1] - x[ed]);
+            if (c[ed] == T(0)) key = T(0);
+            x[i] = r[i] - a[i] * x[st - 1] - c[i] * key;
+        }
+        __syncthreads();
+    } else {
+        cta_cr(sa, sc, sr, sx, m);  // src/tpr.cpp:263-275
+        for (int j = threadIdx.x; j < m; j += blockDim.x)
+            x[j * s + s - 1] = sx[j];
+        // restore: even slice-local rows from the untouched inputs, odd
+        // rows keep their post-stage-1 values (src/tpr.cpp:236-325,381-387)
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            if (((i & (s - 1)) & 1) == 0) {
+                a[i] = ga[i];
+                c[i] = gc[i];
+                r[i] = gr[i];
+            }
+        }
+        __syncthreads();
+        const int ls = ilog2(s);
+        for (int p = ls - 1; p >= 0; p--) {  // src/tpr.cpp:277-308
+            const int u = 1 << p;
+            const int per = s / (2 * u);  // rows per slice at this level
+            for (int t = threadIdx.x; t < m * per; t += blockDim.x) {
+                int j = t / per, q = t - j * per;
+                int i = j * s + u - 1 + 2 * u * q;
+                T xu = (i - u < 0) ? T(0) : x[i - u];
+                x[i] = r[i] - a[i] * xu - c[i] * x[i + u];
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) gx[i] = x[i];
+}
+
+// Standalone CR / PCR on one system per CTA (src/cr.cpp, src/pcr.cpp).
+template <typename T, int KIND>
+__global__ void __launch_bounds__(kThreads)
+fused_crpcr(const T *__restrict__ ga, const T *__restrict__ gc,
+            const T *__restrict__ gr, T *__restrict__ gx, int n,
+            long long stride) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sm = reinterpret_cast<T *>(smem_raw);
+    T *a = sm, *c = sm + n, *r = sm + 2 * n, *x = sm + 3 * n;
+    const long long base = (long long)blockIdx.x * stride;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        a[i] = ga[base + i];
+        c[i] = gc[base + i];
+        r[i] = gr[base + i];
+    }
+    __syncthreads();
+    if (KIND == TPRGB_PCR) {
+        cta_pcr(a, c, r, n);
+        for (int i = threadIdx.x; i < n; i += blockDim.x) gx[base + i] = r[i];
+    } else {
+        cta_cr(a, c, r, x, n);
+        for (int i = threadIdx.x; i < n; i += blockDim.x) gx[base + i] = x[i];
+    }
+}
+
+// ---- sliced shape (large systems) ---------------------------------------
+// workspace per system: wa, wc, wr [n] (rows after stage 1 and the E_st
+// update), then ba, bc, br [m] (E_st backups, PTPR only).
+template <typename T, int KIND>
+__global__ void __launch_bounds__(kThreads)
+sliced_stage1(const T *__restrict__ ga, const T *__restrict__ gc,
+              const T *__restrict__ gr, T *__restrict__ work, int n, int s,
+              long long stride) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *a = reinterpret_cast<T *>(smem_raw), *c = a + s, *r = c + s;
+    const int m = n / s, j = blockIdx.x;
+    const long long base = (long long)blockIdx.y * stride + (long long)j * s;
+    T *wbase = work + (long long)blockIdx.y * (3LL * n + 3LL * m);
+    for (int i = threadIdx.x; i < s; i += blockDim.x) {
+        a[i] = ga[base + i];
+        c[i] = gc[base + i];
+        r[i] = gr[base + i];
+    }
+    __syncthreads();
+    if (KIND == TPRGB_PTPR)
+        ptpr_stage1(a, c, r, s, s);
+    else
+        tpr_stage1(a, c, r, s, s);
+    if (threadIdx.x == 0) {
+        if (KIND == TPRGB_PTPR) {
+            wbase[3LL * n + j] = a[0];
+            wbase[3LL * n + m + j] = c[0];
+            wbase[3LL * n + 2 * m + j] = r[0];
+        }
+        est_update(a, c, r, 0, s - 1);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < s; i += blockDim.x) {
+        wbase[(long long)j * s + i] = a[i];
+        wbase[(long long)n + j * s + i] = c[i];
+        wbase[2LL * n + j * s + i] = r[i];
+    }
+}
+
+template <typename T, int KIND>
+__global__ void __launch_bounds__(kThreads)
+sliced_stage2(const T *__restrict__ work, T *__restrict__ gx, int n, int s,
+              long long stride) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int m = n / s;
+    T *sa = reinterpret_cast<T *>(smem_raw), *sc = sa + m, *sr = sc + m,
+      *sx = sr + m;
+    const T *wa = work + (long long)blockIdx.x * (3LL * n + 3LL * m);
+    const T *wc = wa + n, *wr = wa + 2LL * n;
+    gx += (long long)blockIdx.x * stride;
+    for (int j = threadIdx.x; j < m; j += blockDim.x) {
+        long long k = (long long)j * s + s - 1;
+        if (j < m - 1)
+            inter_eq(wa[k], wc[k], wr[k], wa[k + 1], wc[k + 1], wr[k + 1],
+                     sa[j], sc[j], sr[j]);
+        else {
+            sa[j] = wa[n - 1];
+            sc[j] = wc[n - 1];
+            sr[j] = wr[n - 1];
+        }
+    }
+    __syncthreads();
+    if (KIND == TPRGB_PTPR) {
+        cta_pcr(sa, sc, sr, m);
+        for (int j = threadIdx.x; j < m; j += blockDim.x)
+            gx[(long long)j * s + s - 1] = sr[j];
+    } else {
+        cta_cr(sa, sc, sr, sx, m);
+        for (int j = threadIdx.x; j < m; j += blockDim.x)
+            gx[(long long)j * s + s - 1] = sx[j];
+    }
+}
+
+template <typename T, int KIND>
+__global__ void __launch_bounds__(kThreads)
+sliced_stage3(const T *__restrict__ ga, const T *__restrict__ gc,
+              const T *__restrict__ gr, const T *__restrict__ work,
+              T *__restrict__ gx, int n, int s, long long stride) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int m = n / s, j = blockIdx.x;
+    const long long sys = (long long)blockIdx.y * stride;
+    const T *wa = work + (long long)blockIdx.y * (3LL * n + 3LL * m);
+    const T *wc = wa + n, *wr = wa + 2LL * n;
+    const long long st = (long long)j * s, ed = st + s - 1;
+    T *x = gx + sys;
+    const T xl = (j == 0) ? T(0) : x[st - 1];
+    if (KIND == TPRGB_PTPR) {
+        const T *ba = wa + 3LL * n;
+        const T aed = wa[ed], ced = wc[ed], red = wr[ed], xed = x[ed];
+        T key = T(1) / ced * (red - aed * xl - xed);
+        if (ced == T(0)) key = T(0);
+        for (int i = threadIdx.x; i < s - 1; i += blockDim.x) {
+            long long g = st + i;
+            T ai = (i == 0) ? ba[j] : wa[g];
+            T ci = (i == 0) ? ba[m + j] : wc[g];
+            T ri = (i == 0) ? ba[2 * m + j] : wr[g];
+            x[g] = ri - ai * xl - ci * key;
+        }
+    } else {
+        T *a = reinterpret_cast<T *>(smem_raw), *c = a + s, *r = c + s;
+        T *xs = r + s;  // xs[0] = x[st-1], xs[1..s] = slice
+        for (int i = threadIdx.x; i < s; i += blockDim.x) {
+            long long g = st + i;
+            bool even = (i & 1) == 0;
+            a[i] = even ? ga[sys + g] : wa[g];
+            c[i] = even ? gc[sys + g] : wc[g];
+            r[i] = even ? gr[sys + g] : wr[g];
+        }
+        if (threadIdx.x == 0) {
+            xs[0] = xl;
+            xs[s] = x[ed];
+        }
+        __syncthreads();
+        const int ls = ilog2(s);
+        for (int p = ls - 1; p >= 0; p--) {
+            const int u = 1 << p;
+            for (int q = threadIdx.x; q < s / (2 * u); q += blockDim.x) {
+                int i = u - 1 + 2 * u * q;
+                // x index i (slice-local) lives at xs[i + 1]
+                xs[i + 1] = r[i] - a[i] * xs[i + 1 - u] - c[i] * xs[i + 1 + u];
+            }
+            __syncthreads();
+        }
+        for (int i = threadIdx.x; i < s - 1; i += blockDim.x)
+            x[st + i] = xs[i + 1];
+    }
+}
+
+template <typename T>
+__global__ void normalize_kernel(long long neq, T *a, const T *diag, T *c,
+                                 T *r) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long step = (long long)gridDim.x * blockDim.x;
+    for (; i < neq; i += step) {
+        T d = diag[i];
+        a[i] = a[i] / d;
+        c[i] = c[i] / d;
+        r[i] = r[i] / d;
+    }
+}
+
+}  // namespace refk
+
+// ---- host side -------------------------------------------------------------
+
+static const size_t kFusedSmemLimit = 200 * 1024;
+
+template <typename T>
+static bool ref_uses_fused(int kind, int n, int s) {
+    if (kind == TPRGB_CR || kind == TPRGB_PCR)
+        return true;
+    return refk::fused_elems(n, s) * (long long)sizeof(T) <=
+               (long long)kFusedSmemLimit &&
+           n <= refk::kThreads * refk::kEpt;
+}
+
+int ref_validate(int kind, int n, int s, int prec) {
+    if (kind < TPRGB_PTPR || kind > TPRGB_PCR)
+        return fail(TPRGB_EINVAL, "unknown solver kind %d", kind);
+    if (prec != TPRGB_F32 && prec != TPRGB_F64)
+        return fail(TPRGB_EINVAL, "unknown precision %d", prec);
+    if (!is_pow2(n))
+        return fail(TPRGB_EINVAL, "n=%d must be a power of two", n);
+    const size_t esz = prec == TPRGB_F32 ? 4 : 8;
+    if (kind == TPRGB_CR || kind == TPRGB_PCR) {
+        if ((size_t)n * 4 * esz > kFusedSmemLimit || n > refk::kThreads * refk::kEpt)
+            return fail(TPRGB_EUNSUPPORTED,
+                        "standalone CR/PCR supports n <= %zu here (n=%d)",
+                        kFusedSmemLimit / (4 * esz), n);
+        return TPRGB_OK;
+    }
+    if (!is_pow2(s) || s < 2 || s > n)
+        return fail(TPRGB_EINVAL,
+                    "s=%d must be a power of two with 2 <= s <= n=%d", s, n);
+    const int m = n / s;
+    bool fused = prec == TPRGB_F32 ? ref_uses_fused<float>(kind, n, s)
+                                   : ref_uses_fused<double>(kind, n, s);
+    if (!fused) {
+        if (s > refk::kThreads * refk::kEpt || (size_t)(3 * s + 2) * esz > kFusedSmemLimit)
+            return fail(TPRGB_EUNSUPPORTED, "slice s=%d too large for one CTA", s);
+        if (m > refk::kThreads * refk::kEpt || (size_t)4 * m * esz > kFusedSmemLimit)
+            return fail(TPRGB_EUNSUPPORTED,
+                        "reduced system m=n/s=%d too large for one CTA", m);
+    }
+    return TPRGB_OK;
+}
+
+size_t ref_workspace_elems(int kind, int n, int s) {
+    if (kind == TPRGB_CR || kind == TPRGB_PCR) return 0;
+    return 3ULL * n + 3ULL * (n / s);
+}
+
+bool ref_needs_workspace(int kind, int n, int s, int prec) {
+    if (kind == TPRGB_CR || kind == TPRGB_PCR) return false;
+    return prec == TPRGB_F32 ? !ref_uses_fused<float>(kind, n, s)
+                             : !ref_uses_fused<double>(kind, n, s);
+}
+
+template <typename T, int KIND>
+static int launch_tpr_kind(int nsys, int n, int s, const T *a, const T *c,
+                           const T *r, T *x, long long stride, T *work,
+                           cudaStream_t st) {
+    const int m = n / s;
+    if (ref_uses_fused<T>(KIND, n, s)) {
+        size_t smem = (size_t)refk::fused_elems(n, s) * sizeof(T);
+        int threads = std::min(refk::kThreads, std::max(64, n));
+        auto k = refk::fused_tpr<T, KIND>;
+        TPRGB_CUDA(cudaFuncSetAttribute(
+            k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k<<<nsys, threads, smem, st>>>(a, c, r, x, n, s, stride);
+        TPRGB_CUDA(cudaGetLastError());
+        return TPRGB_OK;
+    }
+    if (work == nullptr)
+        return fail(TPRGB_EINVAL, "sliced solve (n=%d, s=%d) needs a workspace",
+                    n, s);
+    {
+        size_t smem = 3ULL * s * sizeof(T);
+        int threads = std::min(refk::kThreads, std::max(64, s));
+        auto k = refk::sliced_stage1<T, KIND>;
+        TPRGB_CUDA(cudaFuncSetAttribute(
+            k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k<<<dim3(m, nsys), threads, smem, st>>>(a, c, r, work, n, s, stride);
+        TPRGB_CUDA(cudaGetLastError());
+    }
+    {
+        size_t smem = 4ULL * m * sizeof(T);
+        int threads = std::min(refk::kThreads, std::max(64, m));
+        auto k = refk::sliced_stage2<T, KIND>;
+        TPRGB_CUDA(cudaFuncSetAttribute(
+            k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k<<<nsys, threads, smem, st>>>(work, x, n, s, stride);
+        TPRGB_CUDA(cudaGetLastError());
+    }
+    {
+        size_t smem = KIND == TPRGB_TPR ? (4ULL * s + 2) * sizeof(T) : 0;
+        int threads = std::min(refk::kThreads, std::max(64, s));
+        auto k = refk::sliced_stage3<T, KIND>;
+        if (smem)
+            TPRGB_CUDA(cudaFuncSetAttribute(
+                k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k<<<dim3(m, nsys), threads, smem, st>>>(a, c, r, work, x, n, s, stride);
+        TPRGB_CUDA(cudaGetLastError());
+    }
+    return TPRGB_OK;
+}
+
+template <typename T>
+static int launch_ref_t(int kind, int nsys, int n, int s, const T *a,
+                        const T *c, const T *r, T *x, long long stride,
+                        T *work, cudaStream_t st) {
+    switch (kind) {
+        case TPRGB_PTPR:
+            return launch_tpr_kind<T, TPRGB_PTPR>(nsys, n, s, a, c, r, x,
+                                                  stride, work, st);
+        case TPRGB_TPR:
+            return launch_tpr_kind<T, TPRGB_TPR>(nsys, n, s, a, c, r, x,
+                                                 stride, work, st);
+        default: {
+            size_t smem = 4ULL * n * sizeof(T);
+            int threads = std::min(refk::kThreads, std::max(64, n));
+            auto k = kind == TPRGB_CR ? refk::fused_crpcr<T, TPRGB_CR>
+                                      : refk::fused_crpcr<T, TPRGB_PCR>;
+            TPRGB_CUDA(cudaFuncSetAttribute(
+                k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k<<<nsys, threads, smem, st>>>(a, c, r, x, n, stride);
+            TPRGB_CUDA(cudaGetLastError());
+            return TPRGB_OK;
+        }
+    }
+}
+
+int launch_ref(int kind, int nsys, int n, int s, int prec, const void *a,
+               const void *c, const void *r, void *x, long long stride,
+               void *work, cudaStream_t st) {
+    if (prec == TPRGB_F32)
+        return launch_ref_t<float>(kind, nsys, n, s, (const float *)a,
+                                   (const float *)c, (const float *)r,
+                                   (float *)x, stride, (float *)work, st);
+    return launch_ref_t<double>(kind, nsys, n, s, (const double *)a,
+                                (const double *)c, (const double *)r,
+                                (double *)x, stride, (double *)work, st);
+}
+
+int launch_normalize(int prec, long long neq, void *a, const void *diag,
+                     void *c, void *r, cudaStream_t st) {
+    int blocks = (int)std::min<long long>((neq + 255) / 256, 152LL * 16);
+    if (blocks < 1) blocks = 1;
+    if (prec == TPRGB_F32)
+        refk::normalize_kernel<float><<<blocks, 256, 0, st>>>(
+            neq, (float *)a, (const float *)diag, (float *)c, (float *)r);
+    else
+        refk::normalize_kernel<double><<<blocks, 256, 0, st>>>(
+            neq, (double *)a, (const double *)diag, (double *)c, (double *)r);
+    TPRGB_CUDA(cudaGetLastError());
+    return TPRGB_OK;
+}
+
+}  // namespace tprgb
