@@ -196,6 +196,14 @@ TPRGB_API int tprgb_batch_solve_host(tprgb_host_ctx *ctx, int nsys, int n,
                                      const float *c, const float *d, void *x,
                                      const tprgb_batch_opts *opts);
 
+/* ---- diagnostics ------------------------------------------------------- */
+/* out[i] = hi[i] + lo[i] as the nearest double, computed on the device by
+ * the same integer bit assembly the batched solver uses for its FP64
+ * output (no reference counterpart; exposed for testing). */
+TPRGB_API int tprgb_diag_pair_to_double(int64_t n, const float *d_hi,
+                                        const float *d_lo, double *d_out,
+                                        void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,75 @@
+"""The FP32-pair -> FP64 bit assembly used for the solver's FP64 output
+(hier::pair_to_double), emulated step for step on the CPU and checked
+against the exact sum, including values at and around powers of two; the
+GPU test runs the device function itself through a diagnostics entry
+point."""
+import ctypes
+
+import numpy as np
+import pytest
+
+
+def _two_sum(a, b):
+    s = np.float32(a + b)
+    bb = np.float32(s - a)
+    e = np.float32(np.float32(a - np.float32(s - bb)) + np.float32(b - bb))
+    return s, e
+
+
+def emulate(hi, lo):
+    s, e = _two_sum(np.float32(hi), np.float32(lo))
+    u = int(np.array(s, np.float32).view(np.uint32))
+    ex = (u >> 23) & 0xFF
+    if ex < 52 or ex == 255:
+        return float(s) + float(e)
+    sign, mant = u & 0x80000000, u & 0x7FFFFF
+    scale = np.array((306 - ex) << 23, np.uint32).view(np.float32)
+    k = int(np.rint(np.float32(e) * scale))
+    if sign:
+        k = -k
+    if mant == 0 and k < 0:
+        k *= 2
+    bits = ((sign | ((ex + 896) << 20) | (mant >> 3)) << 32) | \
+        ((mant & 7) << 29)
+    bits = (bits + k) & ((1 << 64) - 1)
+    return float(np.array(bits, np.uint64).view(np.float64))
+
+
+def cases(seed=0, n=20000):
+    rng = np.random.default_rng(seed)
+    hi = (rng.uniform(-1, 1, n) * 10.0 ** rng.integers(-12, 12, n)
+          ).astype(np.float32)
+    lo = (hi * rng.uniform(-2.0 ** -22, 2.0 ** -22, n)).astype(np.float32)
+    extra = []
+    for e in range(-30, 30):
+        p = np.float32(2.0 ** e)
+        for f in (1, -1):
+            for r in (-2.0 ** -25, -2.0 ** -26, 2.0 ** -25, -0.75 * 2.0 ** -24,
+                      0.0):
+                extra.append((np.float32(f * p), np.float32(f * p * r)))
+    extra += [(0.0, 1e-30), (1e-40, 0.0), (3.0, 0.0), (1e-30, 1e-38)]
+    eh = np.array([x for x, _ in extra], np.float32)
+    el = np.array([y for _, y in extra], np.float32)
+    return np.concatenate([hi, eh]), np.concatenate([lo, el])
+
+
+def test_emulated_assembly_is_exact():
+    hi, lo = cases()
+    for h, l in zip(hi, lo):
+        assert emulate(h, l) == float(h) + float(l), (h, l)
+
+
+@pytest.mark.gpu
+def test_device_assembly_matches(cuda, lib):
+    torch = cuda
+    hi, lo = cases(1)
+    dh = torch.from_numpy(hi).cuda()
+    dl = torch.from_numpy(lo).cuda()
+    out = torch.empty(len(hi), dtype=torch.float64, device="cuda")
+    rc = lib.tprgb_diag_pair_to_double(len(hi), ctypes.c_void_p(dh.data_ptr()),
+                                       ctypes.c_void_p(dl.data_ptr()),
+                                       ctypes.c_void_p(out.data_ptr()), None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    want = hi.astype(np.float64) + lo.astype(np.float64)
+    np.testing.assert_array_equal(out.cpu().numpy(), want)

@@ -34,6 +34,7 @@ def _declare(L):
         "tprgb_host_ctx_destroy": (i, [vp]),
         "tprgb_batch_solve_host": (i, [vp, i, i, vp, vp, vp, vp, vp,
                                        C.POINTER(BatchOpts)]),
+        "tprgb_diag_pair_to_double": (i, [C.c_int64, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         if hasattr(L, name):

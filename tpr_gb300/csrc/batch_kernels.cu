@@ -250,8 +250,8 @@ batch_uniform(const float *__restrict__ ga, const float *__restrict__ gb,
                 v0 = xd[2 * i];
                 v1 = xd[2 * i + 1];
             } else {
-                v0 = (double)xh[2 * i] + (double)xlo[2 * i];
-                v1 = (double)xh[2 * i + 1] + (double)xlo[2 * i + 1];
+                v0 = hier::pair_to_double(xh[2 * i], xlo[2 * i]);
+                v1 = hier::pair_to_double(xh[2 * i + 1], xlo[2 * i + 1]);
             }
             o[i] = make_double2(v0, v1);
         }
@@ -326,3 +326,27 @@ int launch_batch_uniform(const BatchArgs &A, const TileConfig &cfg,
 }
 
 }  // namespace tprgb
+
+namespace tprgb {
+namespace bk {
+__global__ void diag_pair_kernel(long long n, const float *hi, const float *lo,
+                                 double *out) {
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = hier::pair_to_double(hi[i], lo[i]);
+}
+}  // namespace bk
+}  // namespace tprgb
+
+extern "C" TPRGB_API int tprgb_diag_pair_to_double(int64_t n, const float *hi,
+                                                   const float *lo, double *out,
+                                                   void *stream) {
+    using namespace tprgb;
+    if (n < 0 || (n > 0 && (!hi || !lo || !out)))
+        return fail(TPRGB_EINVAL, "bad arguments");
+    if (n == 0) return TPRGB_OK;
+    long long blocks = (n + 255) / 256;
+    bk::diag_pair_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(
+        n, hi, lo, out);
+    TPRGB_CUDA(cudaGetLastError());
+    return TPRGB_OK;
+}
