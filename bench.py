@@ -188,6 +188,8 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     T.load(build_if_missing=False) if os.path.exists(T.LIB_PATH) else T.load()
+    from tpr_gb300 import autotune
+    tuned = autotune.apply()
 
     bt = G.uniform_batch(NSYS, N, 1_000_000 * (rank + 1), "dominant")
     dev = [torch.from_numpy(v).cuda() for v in (bt.a, bt.b, bt.c, bt.d)]
@@ -289,6 +291,9 @@ def run_ours(args):
             "config": {"workload": WORKLOAD, "nsys_per_gpu": NSYS, "n": N,
                        "s": SLICE, "refine_steps": REFINE,
                        "residual": "compensated FP32",
+                       "tile": dict(zip(("eq_per_thread", "threads_per_cta"),
+                                        B.tile_for(N))),
+                       "tuned_entries": tuned,
                        "x": "FP64", "parallelism": f"replicas x{world}",
                        "l2": "inputs 268 MB > 129 MB L2 (no flush needed)"},
             "rel_l2_max": worst, "rel_l2_max_e2e": worst_e2e,

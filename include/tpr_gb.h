@@ -170,8 +170,10 @@ typedef struct tprgb_batch_opts {
 TPRGB_API int tprgb_batch_opts_default(tprgb_batch_opts *opts);
 
 /* Solve nsys systems of size n laid out back to back (system k at element
- * k*n of every array).  n a power of two, 16 <= n <= 8192.  Asynchronous on
- * `stream`; allocates nothing; can be captured in a CUDA graph. */
+ * k*n of every array).  n a power of two with 2*L <= n <= L * threads per
+ * CTA (8192 with the default tiles); larger systems go through a plan.
+ * Asynchronous on `stream`; allocates nothing; can be captured in a CUDA
+ * graph. */
 TPRGB_API int tprgb_batch_solve(int nsys, int n, const float *d_a,
                                 const float *d_b, const float *d_c,
                                 const float *d_d, void *d_x,
@@ -195,6 +197,143 @@ TPRGB_API int tprgb_batch_solve_host(tprgb_host_ctx *ctx, int nsys, int n,
                                      const float *a, const float *b,
                                      const float *c, const float *d, void *x,
                                      const tprgb_batch_opts *opts);
+
+/* ---- tile table (filled by the autotuner, tpr_gb300/autotune.py) ------
+ * Tile of the uniform kernel for systems of size n: equations per thread
+ * (4 or 8) and threads per CTA.  Also gives the equations per thread the
+ * uneven-batch plans use for that size. */
+TPRGB_API int tprgb_tune_set(int n, int eq_per_thread, int threads_per_cta);
+TPRGB_API int tprgb_tune_get(int n, int *eq_per_thread,
+                             int *threads_per_cta);
+TPRGB_API int tprgb_tune_clear(void);
+
+/* ---- uneven batches: plan + persistent queue kernel ---------------------
+ * A plan fixes the sizes and offsets of a batch of systems (any mix of
+ * power-of-two n, 16 <= n <= 32 * CTA tile); tprgb_plan_execute solves
+ * them in one cooperative launch of a persistent kernel whose CTAs pull
+ * work items (largest systems first) from a device queue.  Systems larger
+ * than one CTA's tile are split over several CTAs that exchange their
+ * reduced rows through the plan's scratch with bounded waits.  Replaces
+ * the reference's one-launch-per-system loop (src/pm.cpp:224-238). */
+typedef struct tprgb_plan tprgb_plan;
+
+/* offsets[k]: first element of system k in every array (multiple of 4);
+ * ns[k]: its size.  opts->threads_per_cta selects 256 or 512 (0 = 256). */
+TPRGB_API int tprgb_plan_create(int nsys, const int64_t *offsets,
+                                const int *ns, const tprgb_batch_opts *opts,
+                                tprgb_plan **out);
+TPRGB_API int tprgb_plan_destroy(tprgb_plan *plan);
+
+/* enable != 0: the first execute with a given set of pointers captures the
+ * reset + launch into a CUDA graph; later executes with the same pointers
+ * replay it. */
+TPRGB_API int tprgb_plan_use_graph(tprgb_plan *plan, int enable);
+
+/* Asynchronous on `stream`; allocates nothing. */
+TPRGB_API int tprgb_plan_execute(tprgb_plan *plan, const float *d_a,
+                                 const float *d_b, const float *d_c,
+                                 const float *d_d, void *d_x, void *stream);
+
+TPRGB_API int tprgb_plan_info(const tprgb_plan *plan, int *nitems, int *grid,
+                              int *nlarge, int *graph_active);
+
+/* After an execute on `stream` (waits for it): sys_status[k] (may be NULL)
+ * is 0 or 1 (non-finite solution) per system in the caller's order;
+ * *device_code the kernel's own status.  Returns TPRGB_ETIMEOUT if a
+ * multi-CTA wait gave up, TPRGB_ENONFINITE if any system is non-finite. */
+TPRGB_API int tprgb_plan_status(tprgb_plan *plan, unsigned *sys_status,
+                                unsigned *device_code, void *stream);
+
+/* ---- seeded synthetic systems generated in device memory ---------------
+ * System k (size d_ns[k], at d_offsets[k], seed d_seeds[k]) is written
+ * into d_a..d_d.  kind: 0 dominant (b = |a|+|c|+U(1,2)), 1 uneven
+ * (+U(0.1,1)), 2 weak (+10^U(-4,-1)).  Counter-based hashing, so the same
+ * (n, seed, kind) always gives the same bits.  No reference counterpart
+ * (the reference generates on the host, src/system.cpp:132-158). */
+TPRGB_API int tprgb_generate_device(int nsys, const int64_t *d_offsets,
+                                    const int *d_ns, const uint64_t *d_seeds,
+                                    int kind, float *d_a, float *d_b,
+                                    float *d_c, float *d_d, void *stream);
+
+/* =========================================================================
+ * Serving loop: continuous batching of solve requests (no reference
+ * counterpart; the reference solves one system per call).  A request is a
+ * set of systems, given either as host arrays or as seeds of the device
+ * generator (state produced and kept on the device).  Requests are
+ * admitted in FIFO order against a device-memory budget, their systems stay
+ * resident until released, and every admitted request is merged into the
+ * next step of the persistent queue kernel; the next step is queued behind
+ * the running one.  Submission is thread-safe.
+ * ====================================================================== */
+typedef struct tprgb_server tprgb_server;
+
+typedef struct tprgb_server_opts {
+    size_t budget_bytes; /* device arena: 24 B per equation (default 8 GiB) */
+    int max_pending;     /* queued, not yet admitted requests (default 2^20) */
+    int refine_steps;    /* default 1                                      */
+    int residual;        /* TPRGB_RESID_DF (default) or TPRGB_RESID_F64     */
+    int threads_per_cta; /* 256 (default) or 512                           */
+} tprgb_server_opts;
+
+typedef struct tprgb_request_info {
+    int status;            /* TPRGB_OK, TPRGB_ENONFINITE, TPRGB_ETIMEOUT... */
+    int nonfinite_systems; /* systems whose solution is not finite          */
+    long long step;        /* the step that solved the request              */
+    double latency_us;     /* submission -> solution resident on the device */
+    long long x_offset;    /* first equation of the request in the arena    */
+    long long neq;         /* equations in the request                      */
+} tprgb_request_info;
+
+typedef struct tprgb_server_stats {
+    long long steps, requests_done, systems_done, equations_done;
+    long long pending, inflight_steps, arena_used_eq, arena_cap_eq;
+} tprgb_server_stats;
+
+TPRGB_API int tprgb_server_opts_default(tprgb_server_opts *opts);
+TPRGB_API int tprgb_server_create(const tprgb_server_opts *opts,
+                                  tprgb_server **out);
+TPRGB_API int tprgb_server_destroy(tprgb_server *srv);
+
+/* Seeded request: system k has size ns[k] (power of two >= 16) and is
+ * generated on the device from seeds[k] (tprgb_generate_device kinds). */
+TPRGB_API int tprgb_server_submit_seeded(tprgb_server *srv, int nsys,
+                                         const int *ns, const uint64_t *seeds,
+                                         int kind, uint64_t *ticket);
+
+/* Host request: systems back to back in a..d (kept valid by the caller
+ * until the request is done); x (may be NULL) receives the FP64 solution. */
+TPRGB_API int tprgb_server_submit_host(tprgb_server *srv, int nsys,
+                                       const int *ns, const float *a,
+                                       const float *b, const float *c,
+                                       const float *d, double *x,
+                                       uint64_t *ticket);
+
+/* Wait (timeout_ms < 0: forever) for a request; returns its status. */
+TPRGB_API int tprgb_server_wait(tprgb_server *srv, uint64_t ticket,
+                                int timeout_ms, tprgb_request_info *info);
+
+/* Copy a finished request's solution (FP64) or its resident system out. */
+TPRGB_API int tprgb_server_fetch(tprgb_server *srv, uint64_t ticket,
+                                 double *x_host);
+TPRGB_API int tprgb_server_fetch_system(tprgb_server *srv, uint64_t ticket,
+                                        float *a, float *b, float *c,
+                                        float *d);
+
+/* Free a finished request's device memory. */
+TPRGB_API int tprgb_server_release(tprgb_server *srv, uint64_t ticket);
+TPRGB_API int tprgb_server_get_stats(tprgb_server *srv,
+                                     tprgb_server_stats *st);
+
+/* Load driver: submits nreq seeded requests with Poisson arrivals at
+ * rate_per_s (<= 0: all at once), each with U{min_sys..max_sys} systems of
+ * size 2^k, k ~ U{kmin..kmax}; waits for and releases them in order.
+ * latencies_us[i] (may be NULL) receives each request's latency, *elapsed_s
+ * first submission -> last completion, *systems_out the systems solved. */
+TPRGB_API int tprgb_server_run_load(tprgb_server *srv, int nreq,
+                                    double rate_per_s, uint64_t seed,
+                                    int min_sys, int max_sys, int kmin,
+                                    int kmax, int kind, double *latencies_us,
+                                    double *elapsed_s, long long *systems_out);
 
 /* ---- diagnostics ------------------------------------------------------- */
 /* out[i] = hi[i] + lo[i] as the nearest double, computed on the device by

@@ -35,6 +35,17 @@ def _declare(L):
         "tprgb_batch_solve_host": (i, [vp, i, i, vp, vp, vp, vp, vp,
                                        C.POINTER(BatchOpts)]),
         "tprgb_diag_pair_to_double": (i, [C.c_int64, vp, vp, vp, vp]),
+        "tprgb_tune_set": (i, [i, i, i]),
+        "tprgb_tune_get": (i, [i, C.POINTER(i), C.POINTER(i)]),
+        "tprgb_tune_clear": (i, []),
+        "tprgb_plan_create": (i, [i, vp, vp, C.POINTER(BatchOpts),
+                                  C.POINTER(vp)]),
+        "tprgb_plan_destroy": (i, [vp]),
+        "tprgb_plan_use_graph": (i, [vp, i]),
+        "tprgb_plan_execute": (i, [vp, vp, vp, vp, vp, vp, vp]),
+        "tprgb_plan_info": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i),
+                                C.POINTER(i)]),
+        "tprgb_plan_status": (i, [vp, vp, C.POINTER(C.c_uint), vp]),
     }
     for name, (res, args) in sig.items():
         if hasattr(L, name):
@@ -124,3 +135,91 @@ class HostContext:
             self.close()
         except Exception:
             pass
+
+
+class Plan:
+    """Uneven batch: systems of any power-of-two sizes at given offsets,
+    solved by the persistent queue kernel (tprgb_plan_*)."""
+
+    def __init__(self, ns, offsets=None, refine_steps: int = 1,
+                 residual: int = RESID_DF, x_f64: bool = True,
+                 threads_per_cta: int = 0, graph: bool = True):
+        ns = np.ascontiguousarray(ns, np.int32)
+        if offsets is None:
+            offsets = np.zeros(len(ns), np.int64)
+            if len(ns) > 1:
+                offsets[1:] = np.cumsum(ns[:-1], dtype=np.int64)
+        offsets = np.ascontiguousarray(offsets, np.int64)
+        self.ns, self.offsets = ns, offsets
+        self.neq = int((offsets + ns).max()) if len(ns) else 0
+        self.x_f64 = x_f64
+        o = opts(refine_steps, residual, x_f64, 0, threads_per_cta)
+        self._h = C.c_void_p()
+        check(load().tprgb_plan_create(len(ns), offsets.ctypes.data,
+                                       ns.ctypes.data, C.byref(o),
+                                       C.byref(self._h)))
+        check(load().tprgb_plan_use_graph(self._h, int(graph)))
+
+    def execute(self, x, a, b, c, d, stream=None):
+        torch = _torch()
+        if stream is None:
+            stream = torch.cuda.current_stream().cuda_stream
+        check(load().tprgb_plan_execute(self._h, a.data_ptr(), b.data_ptr(),
+                                        c.data_ptr(), d.data_ptr(),
+                                        x.data_ptr(), stream))
+
+    def info(self):
+        v = [C.c_int() for _ in range(4)]
+        check(load().tprgb_plan_info(self._h, *[C.byref(t) for t in v]))
+        return dict(zip(("items", "grid", "multi_cta_systems", "graph"),
+                        [t.value for t in v]))
+
+    def status(self, stream=None):
+        """(rc, per-system status array, device code) after an execute."""
+        torch = _torch()
+        if stream is None:
+            stream = torch.cuda.current_stream().cuda_stream
+        st = np.zeros(len(self.ns), np.uint32)
+        code = C.c_uint()
+        rc = load().tprgb_plan_status(self._h, st.ctypes.data, C.byref(code),
+                                      stream)
+        return rc, st, code.value
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            load().tprgb_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solve_plan_host(batch, refine_steps: int = 1, residual: int = RESID_DF,
+                    x_f64: bool = True, threads_per_cta: int = 0,
+                    graph: bool = False, repeats: int = 1):
+    """Solve a generate.Batch (any sizes) through a plan; returns (x, plan
+    status tuple)."""
+    torch = _torch()
+    p = Plan(batch.ns, batch.offsets, refine_steps, residual, x_f64,
+             threads_per_cta, graph)
+    dev = [torch.from_numpy(v).cuda() for v in (batch.a, batch.b, batch.c,
+                                                  batch.d)]
+    x = torch.empty(batch.neq, dtype=torch.float64 if x_f64 else
+                    torch.float32, device="cuda")
+    for _ in range(repeats):
+        p.execute(x, *dev)
+    torch.cuda.synchronize()
+    st = p.status()
+    out = x.cpu().numpy()
+    p.close()
+    return out, st
+
+
+def tile_for(n: int):
+    """(equations per thread, threads per CTA) the library uses for n."""
+    L, nt = C.c_int(), C.c_int()
+    check(load().tprgb_tune_get(n, C.byref(L), C.byref(nt)))
+    return L.value, nt.value

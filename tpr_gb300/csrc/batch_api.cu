@@ -15,6 +15,16 @@ TileConfig default_tile(int n) {
     return TileConfig{8, 1024};
 }
 
+// Tuned tiles per log2(n) (set by the autotuner through tprgb_tune_set).
+static TileConfig g_tuned[32];
+static bool g_has_tuned[32];
+
+TileConfig tuned_tile(int n) {
+    int k = ilog2(n);
+    if (k >= 0 && k < 32 && g_has_tuned[k]) return g_tuned[k];
+    return default_tile(n);
+}
+
 }  // namespace tprgb
 
 using namespace tprgb;
@@ -28,6 +38,29 @@ TPRGB_API int tprgb_batch_opts_default(tprgb_batch_opts *o) {
     o->x_f64 = 1;
     o->eq_per_thread = 0;
     o->threads_per_cta = 0;
+    return TPRGB_OK;
+}
+
+TPRGB_API int tprgb_tune_set(int n, int eq_per_thread, int threads_per_cta) {
+    TileConfig c{eq_per_thread, threads_per_cta};
+    int rc = batch_config_check(n, c);
+    if (rc) return rc;
+    int k = ilog2(n);
+    g_tuned[k] = c;
+    g_has_tuned[k] = true;
+    return TPRGB_OK;
+}
+
+TPRGB_API int tprgb_tune_get(int n, int *eq_per_thread, int *threads_per_cta) {
+    if (!is_pow2(n)) return fail(TPRGB_EINVAL, "n=%d not a power of two", n);
+    TileConfig c = tuned_tile(n);
+    if (eq_per_thread) *eq_per_thread = c.L;
+    if (threads_per_cta) *threads_per_cta = c.nt;
+    return TPRGB_OK;
+}
+
+TPRGB_API int tprgb_tune_clear(void) {
+    for (int k = 0; k < 32; k++) g_has_tuned[k] = false;
     return TPRGB_OK;
 }
 
@@ -52,7 +85,7 @@ TPRGB_API int tprgb_batch_solve(int nsys, int n, const float *d_a,
                           (const void *)d_x})
         if (((uintptr_t)p & 15) != 0)
             return fail(TPRGB_EINVAL, "device arrays must be 16-byte aligned");
-    TileConfig cfg = default_tile(n);
+    TileConfig cfg = tuned_tile(n);
     if (o.eq_per_thread) cfg.L = o.eq_per_thread;
     if (o.threads_per_cta) cfg.nt = o.threads_per_cta;
     BatchArgs A{d_a, d_b, d_c, d_d, d_x, nsys, n, o.refine_steps, o.residual,

@@ -1,0 +1,371 @@
+// Tile solver shared by the uniform batched kernel and the persistent
+// queue kernel: a CTA of NT threads solves either several whole systems
+// (T = n / L threads each) or one part of a system that spans several CTAs
+// (then the CTAs exchange their boundary rows through global scratch).
+#pragma once
+
+#include "common.cuh"
+#include "hier.cuh"
+
+namespace tprgb {
+namespace tile {
+
+using hier::Chunk;
+using hier::Row;
+
+constexpr unsigned kSpinLimit = 1u << 23;  // ~1 s with the back-off below
+
+struct SegRows {
+    Row R0, R1;
+};
+
+// Shared memory of one tile.
+template <int NT>
+struct Smem {
+    SegRows rows[NT / 32];
+    float2 x[NT / 32];
+    float4 edge[2 * (NT / 32)];
+    float2 part_x;  // this part's first / last unknown (multi-CTA systems)
+    int ok;
+};
+
+// Multi-CTA system context.  Scratch per system: counter, then rows
+// [2 parity][32 parts][8 floats] and edges [2 parity][32 parts][4 floats].
+struct Part {
+    int on, P, p;
+    unsigned *counter;
+    float *rows, *edges;
+    unsigned round;
+    DeviceStatus *status;
+    int item;
+};
+
+constexpr int kScratchFloats = 4 + 2 * 32 * 8 + 2 * 32 * 4;  // per system
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Barrier between the CTAs holding the parts of one system.  Bounded: on
+// timeout it records TPRGB_ETIMEOUT and returns false (results of that
+// system are then invalid, the kernel still finishes).
+template <int NT>
+__device__ bool part_barrier(Part &pc, Smem<NT> &sm, int where) {
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        atomicAdd(pc.counter, 1u);
+        const unsigned target = (pc.round + 1u) * (unsigned)pc.P;
+        unsigned it = 0, ns = 32;
+        int ok = 1;
+        while (ld_acquire(pc.counter) < target) {
+            if (++it > kSpinLimit) {
+                ok = 0;
+                atomicCAS(&pc.status->code, 0u, (unsigned)TPRGB_ETIMEOUT);
+                pc.status->where = (unsigned)where;
+                pc.status->detail = (unsigned)pc.item;
+                break;
+            }
+            __nanosleep(ns);
+            if (ns < 256) ns <<= 1;
+        }
+        __threadfence();
+        sm.ok = ok;
+    }
+    __syncthreads();
+    pc.round++;
+    return sm.ok != 0;
+}
+
+// Hierarchical solve.  T: threads of this system inside the CTA (T <= NT;
+// T == NT for a part of a multi-CTA system), a compile-time power of two so
+// that segment widths and lane arithmetic fold to constants.  All threads
+// of the CTA call this (it has CTA barriers when T > 32).
+template <int L, int NT, int T>
+__device__ __forceinline__ void solve(const float (&a)[L], const float (&b)[L],
+                                      const float (&c)[L], const float (&d)[L],
+                                      float (&x)[L], Smem<NT> &sm, Part &pc) {
+    constexpr int K = T < 32 ? T : 32;
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int q = lane & (K - 1);
+    Chunk<L> ck;
+    hier::level0<L>(a, b, c, d, ck);
+    Row R0 = ck.F, R1 = ck.E;
+    hier::seg_reduce_k<K>(R0, R1, q);
+    float xf, xl;
+    if (T <= 32) {
+        hier::seg_top_k<K>(R0, R1, xf, xl);
+    } else {
+        constexpr int W = T > 32 ? T / 32 : 1;
+        const int warp = tid >> 5;
+        const int sys_warp0 = warp & ~(W - 1);
+        const int w = warp - sys_warp0;
+        if (q == 0) sm.rows[warp].R0 = R0;
+        if (q == 31) sm.rows[warp].R1 = R1;
+        __syncthreads();
+        Row S0{0.f, 0.f, 0.f}, S1{0.f, 0.f, 0.f};
+        const int q2 = lane & (W - 1);
+        if (w == 0) {
+            if (lane < W) {
+                S0 = sm.rows[sys_warp0 + lane].R0;
+                S1 = sm.rows[sys_warp0 + lane].R1;
+            }
+            hier::seg_reduce_k<W>(S0, S1, q2);
+        }
+        float yf = 0.f, yl = 0.f;
+        if (!pc.on) {
+            if (w == 0) hier::seg_top_k<W>(S0, S1, yf, yl);
+        } else {
+            // level 3: this CTA's two boundary rows -> scratch, barrier,
+            // every part solves the 2P-row system redundantly
+            const unsigned par = pc.round & 1u;
+            if (warp == 0 && lane == 0) {
+                float4 *dst = reinterpret_cast<float4 *>(pc.rows + (par * 32 + pc.p) * 8);
+                __stcg(dst, make_float4(S0.a, S0.c, S0.d, 0.f));
+            }
+            if (warp == 0 && lane == W - 1) {
+                float4 *dst = reinterpret_cast<float4 *>(pc.rows + (par * 32 + pc.p) * 8 + 4);
+                __stcg(dst, make_float4(S1.a, S1.c, S1.d, 0.f));
+            }
+            part_barrier<NT>(pc, sm, 1);
+            if (warp == 0) {
+                const int P = pc.P;
+                Row U0{0.f, 0.f, 0.f}, U1{0.f, 0.f, 0.f};
+                if (lane < P) {
+                    const float4 *src = reinterpret_cast<const float4 *>(pc.rows + (par * 32 + lane) * 8);
+                    float4 v0 = __ldcg(src), v1 = __ldcg(src + 1);
+                    U0 = Row{v0.x, v0.y, v0.z};
+                    U1 = Row{v1.x, v1.y, v1.z};
+                }
+                const int q3 = lane & (P - 1);
+                hier::seg_reduce(U0, U1, q3, P);
+                float zf, zl, z0, z1;
+                hier::seg_top(U0, U1, q3, P, zf, zl);
+                hier::seg_back(U0, U1, q3, P, zf, zl, z0, z1);
+                yf = __shfl_sync(0xffffffffu, z0, pc.p);
+                yl = __shfl_sync(0xffffffffu, z1, pc.p);
+            }
+        }
+        if (w == 0) {
+            float y0, y1;
+            hier::seg_back(S0, S1, q2, W, yf, yl, y0, y1);
+            if (lane < W) sm.x[sys_warp0 + lane] = make_float2(y0, y1);
+        }
+        __syncthreads();
+        float2 v = sm.x[warp];
+        xf = v.x;
+        xl = v.y;
+    }
+    float x0, x1;
+    hier::seg_back(R0, R1, q, K, xf, xl, x0, x1);
+    hier::level0_back<L>(ck, x0, x1, x);
+}
+
+// x[-1] and x[L] of this thread's chunk (hi, lo pairs), zero outside the
+// system.  t: thread index within the system's threads of this CTA.
+template <int NT, int T>
+__device__ __forceinline__ void neighbours(float hfirst, float hlast,
+                                           float lfirst, float llast, int t,
+                                           float &hm, float &lm, float &hp,
+                                           float &lp, Smem<NT> &sm, Part &pc) {
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    constexpr int K = T < 32 ? T : 32;
+    hm = __shfl_up_sync(0xffffffffu, hlast, 1, K);
+    lm = __shfl_up_sync(0xffffffffu, llast, 1, K);
+    hp = __shfl_down_sync(0xffffffffu, hfirst, 1, K);
+    lp = __shfl_down_sync(0xffffffffu, lfirst, 1, K);
+    if (T > 32) {
+        const int warp = tid >> 5;
+        if (lane == 0) sm.edge[2 * warp] = make_float4(hfirst, lfirst, 0.f, 0.f);
+        if (lane == 31) sm.edge[2 * warp + 1] = make_float4(hlast, llast, 0.f, 0.f);
+        __syncthreads();
+        if (lane == 0 && t > 0) {
+            float4 v = sm.edge[2 * (warp - 1) + 1];
+            hm = v.x;
+            lm = v.y;
+        }
+        if (lane == 31 && t < T - 1) {
+            float4 v = sm.edge[2 * (warp + 1)];
+            hp = v.x;
+            lp = v.y;
+        }
+        __syncthreads();
+    }
+    if (pc.on) {
+        // neighbouring parts' edge values through scratch
+        const unsigned par = pc.round & 1u;
+        float2 *mine = reinterpret_cast<float2 *>(pc.edges + (par * 32 + pc.p) * 4);
+        if (t == 0) __stcg(mine, make_float2(hfirst, lfirst));
+        if (t == T - 1) __stcg(mine + 1, make_float2(hlast, llast));
+        part_barrier<NT>(pc, sm, 2);
+        if (t == 0) {
+            if (pc.p > 0) {
+                float4 v = __ldcg(reinterpret_cast<const float4 *>(
+                    pc.edges + (par * 32 + pc.p - 1) * 4));
+                hm = v.z;
+                lm = v.w;
+            } else {
+                hm = 0.f;
+                lm = 0.f;
+            }
+        }
+        if (t == T - 1) {
+            if (pc.p < pc.P - 1) {
+                float4 v = __ldcg(reinterpret_cast<const float4 *>(
+                    pc.edges + (par * 32 + pc.p + 1) * 4));
+                hp = v.x;
+                lp = v.y;
+            } else {
+                hp = 0.f;
+                lp = 0.f;
+            }
+        }
+    } else {
+        if (t == 0) {
+            hm = 0.f;
+            lm = 0.f;
+        }
+        if (t == T - 1) {
+            hp = 0.f;
+            lp = 0.f;
+        }
+    }
+}
+
+template <int L>
+__device__ __forceinline__ void load_chunk(const float *__restrict__ p,
+                                           float (&v)[L]) {
+    const float4 *q = reinterpret_cast<const float4 *>(p);
+#pragma unroll
+    for (int i = 0; i < L / 4; i++) {
+        float4 t = __ldg(q + i);
+        v[4 * i + 0] = t.x;
+        v[4 * i + 1] = t.y;
+        v[4 * i + 2] = t.z;
+        v[4 * i + 3] = t.w;
+    }
+}
+
+// Whole tile: load, solve, refine, store.  MODE: 0 plain FP32, 1 refine
+// with compensated residual, 2 refine with native FP64 residual.
+// first_eq / last_eq: this thread's chunk holds the system's first / last
+// equation.  Returns true if every x of this thread is finite.
+template <int L, int NT, int T, int MODE>
+__device__ __forceinline__ bool run_tile(
+    const float *__restrict__ ga, const float *__restrict__ gb,
+    const float *__restrict__ gc, const float *__restrict__ gd,
+    void *__restrict__ gx, long long base, bool active, int t, bool first_eq,
+    bool last_eq, int refine_steps, int x_f64, Smem<NT> &sm, Part &pc) {
+    float a[L], b[L], c[L], d[L];
+    if (active) {
+        load_chunk<L>(ga + base, a);
+        load_chunk<L>(gb + base, b);
+        load_chunk<L>(gc + base, c);
+        load_chunk<L>(gd + base, d);
+    } else {
+#pragma unroll
+        for (int i = 0; i < L; i++) {
+            a[i] = 0.f;
+            b[i] = 1.f;
+            c[i] = 0.f;
+            d[i] = 0.f;
+        }
+    }
+    if (first_eq) a[0] = 0.f;     // a[0] of a system takes no part
+    if (last_eq) c[L - 1] = 0.f;  // nor does c[n-1]
+
+    float xh[L];
+    solve<L, NT, T>(a, b, c, d, xh, sm, pc);
+
+    float xlo[L];
+    double xd[L];
+#pragma unroll
+    for (int i = 0; i < L; i++) {
+        xlo[i] = 0.f;
+        if (MODE == 2) xd[i] = (double)xh[i];
+    }
+    if (MODE != 0) {
+        for (int step = 0; step < refine_steps; step++) {
+            float r[L];
+            float hm, lm, hp, lp;
+            if (MODE == 1) {
+                neighbours<NT, T>(xh[0], xh[L - 1], xlo[0], xlo[L - 1], t, hm,
+                                  lm, hp, lp, sm, pc);
+#pragma unroll
+                for (int i = 0; i < L; i++) {
+                    float xmh = i > 0 ? xh[i - 1] : hm;
+                    float xml = i > 0 ? xlo[i - 1] : lm;
+                    float xph = i < L - 1 ? xh[i + 1] : hp;
+                    float xpl = i < L - 1 ? xlo[i + 1] : lp;
+                    r[i] = hier::residual_df(a[i], b[i], c[i], d[i], xmh, xml,
+                                             xh[i], xlo[i], xph, xpl);
+                }
+            } else {
+                float fh = (float)xd[0], fl = (float)(xd[0] - (double)fh);
+                float lh = (float)xd[L - 1], ll = (float)(xd[L - 1] - (double)lh);
+                neighbours<NT, T>(fh, lh, fl, ll, t, hm, lm, hp, lp, sm, pc);
+                const double xm = (double)hm + (double)lm;
+                const double xp = (double)hp + (double)lp;
+#pragma unroll
+                for (int i = 0; i < L; i++) {
+                    double xl_ = i > 0 ? xd[i - 1] : xm;
+                    double xr_ = i < L - 1 ? xd[i + 1] : xp;
+                    double rr = (double)d[i];
+                    rr = fma(-(double)b[i], xd[i], rr);
+                    rr = fma(-(double)a[i], xl_, rr);
+                    rr = fma(-(double)c[i], xr_, rr);
+                    r[i] = (float)rr;
+                }
+            }
+            float dx[L];
+            solve<L, NT, T>(a, b, c, r, dx, sm, pc);
+#pragma unroll
+            for (int i = 0; i < L; i++) {
+                if (MODE == 1)
+                    xlo[i] += dx[i];
+                else
+                    xd[i] += (double)dx[i];
+            }
+        }
+    }
+
+    bool finite = true;
+    if (!active) return true;
+    if (x_f64) {
+        double2 *o = reinterpret_cast<double2 *>((double *)gx + base);
+#pragma unroll
+        for (int i = 0; i < L / 2; i++) {
+            double v0, v1;
+            if (MODE == 2) {
+                v0 = xd[2 * i];
+                v1 = xd[2 * i + 1];
+            } else {
+                v0 = hier::pair_to_double(xh[2 * i], xlo[2 * i]);
+                v1 = hier::pair_to_double(xh[2 * i + 1], xlo[2 * i + 1]);
+            }
+            finite = finite && isfinite(xh[2 * i]) && isfinite(xh[2 * i + 1]);
+            o[i] = make_double2(v0, v1);
+        }
+    } else {
+        float4 *o = reinterpret_cast<float4 *>((float *)gx + base);
+#pragma unroll
+        for (int i = 0; i < L / 4; i++) {
+            float v[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                v[j] = MODE == 2 ? (float)xd[4 * i + j]
+                                 : xh[4 * i + j] + xlo[4 * i + j];
+                finite = finite && isfinite(v[j]);
+            }
+            o[i] = make_float4(v[0], v[1], v[2], v[3]);
+        }
+    }
+    return finite;
+}
+
+}  // namespace tile
+}  // namespace tprgb
