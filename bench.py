@@ -291,8 +291,8 @@ def run_ours(args):
             "config": {"workload": WORKLOAD, "nsys_per_gpu": NSYS, "n": N,
                        "s": SLICE, "refine_steps": REFINE,
                        "residual": "compensated FP32",
-                       "tile": dict(zip(("eq_per_thread", "threads_per_cta"),
-                                        B.tile_for(N))),
+                       "tile": dict(zip(("eq_per_thread", "threads_per_cta",
+                                         "variant"), B.tile_for(N))),
                        "tuned_entries": tuned,
                        "x": "FP64", "parallelism": f"replicas x{world}",
                        "l2": "inputs 268 MB > 129 MB L2 (no flush needed)"},

@@ -164,6 +164,9 @@ typedef struct tprgb_batch_opts {
     int x_f64;           /* 1: x is double[neq]; 0: x is float[neq]         */
     int eq_per_thread;   /* 0: tuned table; otherwise 4 or 8                */
     int threads_per_cta; /* 0: tuned table; otherwise 128, 256, 512, 1024   */
+    int variant;         /* 0: tuned table; 1: inputs loaded to registers;
+                            2: inputs staged in shared memory by TMA bulk
+                               copies (persistent CTAs, 256 or 512 threads) */
 } tprgb_batch_opts;
 
 /* Defaults: 1 refinement step, compensated residual, FP64 x, tuned tile. */
@@ -202,9 +205,10 @@ TPRGB_API int tprgb_batch_solve_host(tprgb_host_ctx *ctx, int nsys, int n,
  * Tile of the uniform kernel for systems of size n: equations per thread
  * (4 or 8) and threads per CTA.  Also gives the equations per thread the
  * uneven-batch plans use for that size. */
-TPRGB_API int tprgb_tune_set(int n, int eq_per_thread, int threads_per_cta);
-TPRGB_API int tprgb_tune_get(int n, int *eq_per_thread,
-                             int *threads_per_cta);
+TPRGB_API int tprgb_tune_set(int n, int eq_per_thread, int threads_per_cta,
+                             int variant);
+TPRGB_API int tprgb_tune_get(int n, int *eq_per_thread, int *threads_per_cta,
+                             int *variant);
 TPRGB_API int tprgb_tune_clear(void);
 
 /* ---- uneven batches: plan + persistent queue kernel ---------------------
@@ -336,6 +340,10 @@ TPRGB_API int tprgb_server_run_load(tprgb_server *srv, int nreq,
                                     double *elapsed_s, long long *systems_out);
 
 /* ---- diagnostics ------------------------------------------------------- */
+/* Status word of the TMA-staged batched kernel: *code = TPRGB_ETIMEOUT if a
+ * bounded wait gave up since the last reset (reset != 0 clears it). */
+TPRGB_API int tprgb_batch_status(unsigned *code, int reset);
+
 /* out[i] = hi[i] + lo[i] as the nearest double, computed on the device by
  * the same integer bit assembly the batched solver uses for its FP64
  * output (no reference counterpart; exposed for testing). */

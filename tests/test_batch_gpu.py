@@ -87,3 +87,30 @@ def test_rejects_bad_arguments(cuda):
     a = torch.zeros(1 << 15, device="cuda")
     with pytest.raises(T.TprError):
         B.solve(a, a, a, a, 1 << 15, eq_per_thread=8, threads_per_cta=256)
+
+
+@pytest.mark.parametrize("n", [16, 64, 256, 1024, 4096])
+@pytest.mark.parametrize("L,nt", [(4, 256), (4, 512), (8, 256), (8, 512)])
+def test_staged_kernel_matches_register_kernel(cuda, port, n, L, nt):
+    """The TMA-staged variant computes the same bits as the register
+    variant (same arithmetic, different data path) and meets 1e-9; the
+    batch ends in a partial tile."""
+    if n < 2 * L or n // L > nt:
+        pytest.skip("tile does not cover this size")
+    nsys = 3 * (nt * L // n) + 1
+    bt = G.uniform_batch(nsys, n, 31 + n, "uneven")
+    xs = B.solve_host(bt, refine_steps=1, eq_per_thread=L, threads_per_cta=nt,
+                      variant=B.STAGED)
+    xr = B.solve_host(bt, refine_steps=1, eq_per_thread=L, threads_per_cta=nt,
+                      variant=B.REGISTERS)
+    np.testing.assert_array_equal(xs, xr)
+    worst, _ = _err(port, bt, xs)
+    assert worst <= 1e-9, worst
+    xp = B.solve_host(bt, refine_steps=0, x_f64=False, eq_per_thread=L,
+                      threads_per_cta=nt, variant=B.STAGED)
+    worst, _ = _err(port, bt, xp)
+    assert worst <= 1e-5, worst
+    import ctypes
+    code = ctypes.c_uint()
+    assert B.load().tprgb_batch_status(ctypes.byref(code), 1) == 0
+    assert code.value == 0

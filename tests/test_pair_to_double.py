@@ -23,12 +23,24 @@ def emulate(hi, lo):
     if ex < 52 or ex == 255:
         return float(s) + float(e)
     sign, mant = u & 0x80000000, u & 0x7FFFFF
-    scale = np.array((306 - ex) << 23, np.uint32).view(np.float32)
-    k = int(np.rint(np.float32(e) * scale))
-    if sign:
-        k = -k
-    if mant == 0 and k < 0:
-        k *= 2
+    ue = int(np.array(e, np.float32).view(np.uint32))
+    ee = (ue >> 23) & 0xFF
+    k = 0
+    if ee != 0:
+        down = ((ue ^ u) & 0x80000000) != 0
+        m = (ue & 0x7FFFFF) | 0x800000
+        sh = ee - ex + 29 + (1 if (mant == 0 and down) else 0)
+        if sh >= 0:
+            kk = m << sh
+        elif sh > -25:
+            r = -sh
+            kk = m >> r
+            rem, half = m & ((1 << r) - 1), 1 << (r - 1)
+            if rem > half or (rem == half and (kk & 1)):
+                kk += 1
+        else:
+            kk = 0
+        k = -kk if down else kk
     bits = ((sign | ((ex + 896) << 20) | (mant >> 3)) << 32) | \
         ((mant & 7) << 29)
     bits = (bits + k) & ((1 << 64) - 1)
@@ -48,6 +60,11 @@ def cases(seed=0, n=20000):
                       0.0):
                 extra.append((np.float32(f * p), np.float32(f * p * r)))
     extra += [(0.0, 1e-30), (1e-40, 0.0), (3.0, 0.0), (1e-30, 1e-38)]
+    # exact halfway cases between doubles (ties to even)
+    for h in (1.0, 1.0 + 2.0 ** -23, -1.0, 1.5, 2.0 ** 20):
+        u = 2.0 ** (np.floor(np.log2(abs(h))) - 53)
+        for m in (1, 3, 5, -1, -3):
+            extra.append((np.float32(h), np.float32(m * u)))
     eh = np.array([x for x, _ in extra], np.float32)
     el = np.array([y for _, y in extra], np.float32)
     return np.concatenate([hi, eh]), np.concatenate([lo, el])

@@ -89,7 +89,7 @@ def test_budget_admission_and_release(cuda):
     never exceeds the budget; completion steps follow submission order."""
     rng = np.random.default_rng(3)
     budget = 48 << 20            # 2M equations
-    reqs = [_req(rng, 64, 10, 13) for _ in range(40)]
+    reqs = [_req(rng, 64, 11, 13) for _ in range(80)]
     assert sum(int(r[0].sum()) for r in reqs) * 24 > 4 * budget
     with Server(budget_bytes=budget) as s:
         cap = s.stats()["arena_cap_eq"]

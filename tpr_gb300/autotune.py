@@ -27,8 +27,10 @@ from . import check, load
 PKG = os.path.dirname(os.path.abspath(__file__))
 TABLE = os.path.join(PKG, "tuned_tiles.json")
 SIZES = [16, 32, 64, 128, 256, 512, 1024, 2048, 4096, 8192]
-CANDIDATES = [(4, 128), (4, 256), (4, 512), (4, 1024),
-              (8, 128), (8, 256), (8, 512), (8, 1024)]
+# (equations per thread, threads per CTA, variant: 1 registers, 2 staged)
+CANDIDATES = [(4, 128, 1), (4, 256, 1), (4, 512, 1), (4, 1024, 1),
+              (8, 128, 1), (8, 256, 1), (8, 512, 1), (8, 1024, 1),
+              (4, 256, 2), (4, 512, 2), (8, 256, 2), (8, 512, 2)]
 
 
 def _device_name():
@@ -36,8 +38,8 @@ def _device_name():
     return torch.cuda.get_device_name(0)
 
 
-def time_tile(n, L, nt, refine_steps=1, eq_per_trial=1 << 24, reps=10,
-              dev_arrays=None):
+def time_tile(n, L, nt, variant=1, refine_steps=1, eq_per_trial=1 << 24,
+              reps=10, dev_arrays=None):
     """Mean milliseconds per launch of the uniform kernel for one tile."""
     import torch
 
@@ -53,7 +55,8 @@ def time_tile(n, L, nt, refine_steps=1, eq_per_trial=1 << 24, reps=10,
     else:
         a, b, c, d = dev_arrays
     x = torch.empty(nsys * n, dtype=torch.float64, device="cuda")
-    o = B.opts(refine_steps=refine_steps, eq_per_thread=L, threads_per_cta=nt)
+    o = B.opts(refine_steps=refine_steps, eq_per_thread=L, threads_per_cta=nt,
+               variant=variant)
     for _ in range(3):
         B.solve_into(x, a, b, c, d, n, o)
     s = torch.cuda.Event(enable_timing=True)
@@ -80,20 +83,21 @@ def tune(sizes=SIZES, refine_steps=1, verbose=True):
         d = torch.rand(nsys * n, device="cuda", generator=g)
         best = None
         trials = {}
-        for L, nt in CANDIDATES:
+        for L, nt, v in CANDIDATES:
             if n < 2 * L or n // L > nt:
                 continue
-            ms, _ = time_tile(n, L, nt, refine_steps, dev_arrays=(a, b, c, d))
-            trials[f"{L}x{nt}"] = ms
-            if best is None or ms < best[2]:
-                best = (L, nt, ms)
+            ms, _ = time_tile(n, L, nt, v, refine_steps,
+                              dev_arrays=(a, b, c, d))
+            trials[f"{L}x{nt}{'s' if v == 2 else ''}"] = ms
+            if best is None or ms < best[3]:
+                best = (L, nt, v, ms)
         table[str(n)] = {"eq_per_thread": best[0], "threads_per_cta": best[1],
-                         "ms": best[2], "systems": nsys,
-                         "systems_per_s": nsys / (best[2] * 1e-3),
+                         "variant": best[2], "ms": best[3], "systems": nsys,
+                         "systems_per_s": nsys / (best[3] * 1e-3),
                          "trials_ms": trials}
         if verbose:
-            print(f"n={n:6d}: best L={best[0]} nt={best[1]} "
-                  f"{best[2]:.4f} ms  {trials}", flush=True)
+            print(f"n={n:6d}: best L={best[0]} nt={best[1]} v={best[2]} "
+                  f"{best[3]:.4f} ms  {trials}", flush=True)
         del a, b, c, d
     return table
 
@@ -121,7 +125,8 @@ def apply(path=TABLE, device_name=None) -> int:
     k = 0
     for n, ent in doc["tiles"].items():
         check(L.tprgb_tune_set(int(n), int(ent["eq_per_thread"]),
-                               int(ent["threads_per_cta"])))
+                               int(ent["threads_per_cta"]),
+                               int(ent.get("variant", 1))))
         k += 1
     return k
 

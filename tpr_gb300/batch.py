@@ -13,7 +13,7 @@ import ctypes as C
 
 import numpy as np
 
-from . import check, load
+from . import check, load  # noqa: F401  (load re-exported)
 
 RESID_DF, RESID_F64 = 0, 1
 
@@ -21,7 +21,7 @@ RESID_DF, RESID_F64 = 0, 1
 class BatchOpts(C.Structure):
     _fields_ = [("refine_steps", C.c_int), ("residual", C.c_int),
                 ("x_f64", C.c_int), ("eq_per_thread", C.c_int),
-                ("threads_per_cta", C.c_int)]
+                ("threads_per_cta", C.c_int), ("variant", C.c_int)]
 
 
 def _declare(L):
@@ -35,8 +35,9 @@ def _declare(L):
         "tprgb_batch_solve_host": (i, [vp, i, i, vp, vp, vp, vp, vp,
                                        C.POINTER(BatchOpts)]),
         "tprgb_diag_pair_to_double": (i, [C.c_int64, vp, vp, vp, vp]),
-        "tprgb_tune_set": (i, [i, i, i]),
-        "tprgb_tune_get": (i, [i, C.POINTER(i), C.POINTER(i)]),
+        "tprgb_tune_set": (i, [i, i, i, i]),
+        "tprgb_tune_get": (i, [i, C.POINTER(i), C.POINTER(i), C.POINTER(i)]),
+        "tprgb_batch_status": (i, [C.POINTER(C.c_uint), i]),
         "tprgb_tune_clear": (i, []),
         "tprgb_plan_create": (i, [i, vp, vp, C.POINTER(BatchOpts),
                                   C.POINTER(vp)]),
@@ -54,8 +55,12 @@ def _declare(L):
             fn.argtypes = args
 
 
+REGISTERS, STAGED = 1, 2
+
+
 def opts(refine_steps: int = 1, residual: int = RESID_DF, x_f64: bool = True,
-         eq_per_thread: int = 0, threads_per_cta: int = 0) -> BatchOpts:
+         eq_per_thread: int = 0, threads_per_cta: int = 0,
+         variant: int = 0) -> BatchOpts:
     o = BatchOpts()
     check(load().tprgb_batch_opts_default(C.byref(o)))
     o.refine_steps = refine_steps
@@ -63,6 +68,7 @@ def opts(refine_steps: int = 1, residual: int = RESID_DF, x_f64: bool = True,
     o.x_f64 = int(bool(x_f64))
     o.eq_per_thread = eq_per_thread
     o.threads_per_cta = threads_per_cta
+    o.variant = variant
     return o
 
 
@@ -219,7 +225,7 @@ def solve_plan_host(batch, refine_steps: int = 1, residual: int = RESID_DF,
 
 
 def tile_for(n: int):
-    """(equations per thread, threads per CTA) the library uses for n."""
-    L, nt = C.c_int(), C.c_int()
-    check(load().tprgb_tune_get(n, C.byref(L), C.byref(nt)))
-    return L.value, nt.value
+    """(equations per thread, threads per CTA, variant) used for size n."""
+    L, nt, v = C.c_int(), C.c_int(), C.c_int()
+    check(load().tprgb_tune_get(n, C.byref(L), C.byref(nt), C.byref(v)))
+    return L.value, nt.value, v.value

@@ -33,6 +33,7 @@ SOURCES = {
     # results match the reference CPU solvers bit for bit
     "ref_kernels.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
     "batch_kernels.cu": [],
+    "batch_tma.cu": [],
     "batch_api.cu": [],
     "plan_kernels.cu": [],
     "gen_kernels.cu": [],

@@ -14,14 +14,17 @@ struct BatchArgs {
     int x_f64;
 };
 
-// Tile shape: L equations per thread, nt threads per CTA.
+// Tile shape: L equations per thread, nt threads per CTA, and the kernel
+// variant (0: inputs loaded straight to registers; 1: TMA-staged ring).
 struct TileConfig {
     int L;
     int nt;
+    int staged = 0;
 };
 
 int batch_config_check(int n, const TileConfig &cfg);
 int launch_batch_uniform(const BatchArgs &A, const TileConfig &cfg,
                          cudaStream_t st);
+int launch_batch_tma(const BatchArgs &A, const TileConfig &cfg, cudaStream_t st);
 
 }  // namespace tprgb

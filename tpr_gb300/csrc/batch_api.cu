@@ -38,11 +38,16 @@ TPRGB_API int tprgb_batch_opts_default(tprgb_batch_opts *o) {
     o->x_f64 = 1;
     o->eq_per_thread = 0;
     o->threads_per_cta = 0;
+    o->variant = 0;
     return TPRGB_OK;
 }
 
-TPRGB_API int tprgb_tune_set(int n, int eq_per_thread, int threads_per_cta) {
-    TileConfig c{eq_per_thread, threads_per_cta};
+TPRGB_API int tprgb_tune_set(int n, int eq_per_thread, int threads_per_cta,
+                             int variant) {
+    if (variant < 0 || variant > 2) return fail(TPRGB_EINVAL, "variant %d", variant);
+    TileConfig c{eq_per_thread, threads_per_cta, variant == 2 ? 1 : 0};
+    if (c.staged && c.nt != 256 && c.nt != 512)
+        return fail(TPRGB_EINVAL, "staged tiles use 256 or 512 threads");
     int rc = batch_config_check(n, c);
     if (rc) return rc;
     int k = ilog2(n);
@@ -51,11 +56,13 @@ TPRGB_API int tprgb_tune_set(int n, int eq_per_thread, int threads_per_cta) {
     return TPRGB_OK;
 }
 
-TPRGB_API int tprgb_tune_get(int n, int *eq_per_thread, int *threads_per_cta) {
+TPRGB_API int tprgb_tune_get(int n, int *eq_per_thread, int *threads_per_cta,
+                             int *variant) {
     if (!is_pow2(n)) return fail(TPRGB_EINVAL, "n=%d not a power of two", n);
     TileConfig c = tuned_tile(n);
     if (eq_per_thread) *eq_per_thread = c.L;
     if (threads_per_cta) *threads_per_cta = c.nt;
+    if (variant) *variant = c.staged ? 2 : 1;
     return TPRGB_OK;
 }
 
@@ -85,11 +92,21 @@ TPRGB_API int tprgb_batch_solve(int nsys, int n, const float *d_a,
                           (const void *)d_x})
         if (((uintptr_t)p & 15) != 0)
             return fail(TPRGB_EINVAL, "device arrays must be 16-byte aligned");
+    if (o.variant < 0 || o.variant > 2)
+        return fail(TPRGB_EINVAL, "unknown kernel variant %d", o.variant);
     TileConfig cfg = tuned_tile(n);
     if (o.eq_per_thread) cfg.L = o.eq_per_thread;
     if (o.threads_per_cta) cfg.nt = o.threads_per_cta;
+    if (o.variant) cfg.staged = o.variant == 2 ? 1 : 0;
     BatchArgs A{d_a, d_b, d_c, d_d, d_x, nsys, n, o.refine_steps, o.residual,
                 o.x_f64};
+    const bool staged_ok = (cfg.nt == 256 || cfg.nt == 512) &&
+                           !(o.residual == TPRGB_RESID_F64 && o.refine_steps > 0);
+    if (cfg.staged && staged_ok)
+        return launch_batch_tma(A, cfg, (cudaStream_t)stream);
+    if (o.variant == 2)
+        return fail(TPRGB_EUNSUPPORTED,
+                    "staged kernel needs 256/512 threads and the compensated residual");
     return launch_batch_uniform(A, cfg, (cudaStream_t)stream);
 }
 

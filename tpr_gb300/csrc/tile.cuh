@@ -367,5 +367,112 @@ __device__ __forceinline__ bool run_tile(
     return finite;
 }
 
+
+// ---- tile runner with the raw system staged in shared memory ---------------
+template <int L>
+__device__ __forceinline__ void lds_chunk(const float *p, float (&v)[L]) {
+    const float4 *q = reinterpret_cast<const float4 *>(p);
+#pragma unroll
+    for (int i = 0; i < L / 4; i++) {
+        float4 t = q[i];
+        v[4 * i + 0] = t.x;
+        v[4 * i + 1] = t.y;
+        v[4 * i + 2] = t.z;
+        v[4 * i + 3] = t.w;
+    }
+}
+
+// Same computation as run_tile, but a, b, c, d are re-read from shared
+// memory (sa..sd: this thread's chunk) each time they are needed instead
+// of being held in registers through the refinement.
+template <int L, int NT, int T, int MODE>
+__device__ __forceinline__ bool run_tile_smem(
+    const float *sa, const float *sb, const float *sc, const float *sd,
+    void *__restrict__ gx, long long base, bool active, int t, bool first_eq,
+    bool last_eq, int refine_steps, int x_f64, Smem<NT> &sm, Part &pc) {
+    auto load4 = [&](float (&a)[L], float (&b)[L], float (&c)[L],
+                     float (&d)[L]) {
+        if (active) {
+            lds_chunk<L>(sa, a);
+            lds_chunk<L>(sb, b);
+            lds_chunk<L>(sc, c);
+            lds_chunk<L>(sd, d);
+        } else {
+#pragma unroll
+            for (int i = 0; i < L; i++) {
+                a[i] = 0.f;
+                b[i] = 1.f;
+                c[i] = 0.f;
+                d[i] = 0.f;
+            }
+        }
+        if (first_eq) a[0] = 0.f;
+        if (last_eq) c[L - 1] = 0.f;
+    };
+    float xh[L];
+    {
+        float a[L], b[L], c[L], d[L];
+        load4(a, b, c, d);
+        solve<L, NT, T>(a, b, c, d, xh, sm, pc);
+    }
+    float xlo[L];
+#pragma unroll
+    for (int i = 0; i < L; i++) xlo[i] = 0.f;
+    if (MODE == 1) {
+        for (int step = 0; step < refine_steps; step++) {
+            float hm, lm, hp, lp;
+            neighbours<NT, T>(xh[0], xh[L - 1], xlo[0], xlo[L - 1], t, hm, lm,
+                              hp, lp, sm, pc);
+            float r[L];
+            {
+                float a[L], b[L], c[L], d[L];
+                load4(a, b, c, d);
+#pragma unroll
+                for (int i = 0; i < L; i++) {
+                    float xmh = i > 0 ? xh[i - 1] : hm;
+                    float xml = i > 0 ? xlo[i - 1] : lm;
+                    float xph = i < L - 1 ? xh[i + 1] : hp;
+                    float xpl = i < L - 1 ? xlo[i + 1] : lp;
+                    r[i] = hier::residual_df(a[i], b[i], c[i], d[i], xmh, xml,
+                                             xh[i], xlo[i], xph, xpl);
+                }
+            }
+            float dx[L];
+            {
+                float a[L], b[L], c[L], d[L];
+                load4(a, b, c, d);
+                solve<L, NT, T>(a, b, c, r, dx, sm, pc);
+            }
+#pragma unroll
+            for (int i = 0; i < L; i++) xlo[i] += dx[i];
+        }
+    }
+    bool finite = true;
+    if (!active) return true;
+    if (x_f64) {
+        double2 *o = reinterpret_cast<double2 *>((double *)gx + base);
+#pragma unroll
+        for (int i = 0; i < L / 2; i++) {
+            double v0 = hier::pair_to_double(xh[2 * i], xlo[2 * i]);
+            double v1 = hier::pair_to_double(xh[2 * i + 1], xlo[2 * i + 1]);
+            finite = finite && isfinite(xh[2 * i]) && isfinite(xh[2 * i + 1]);
+            o[i] = make_double2(v0, v1);
+        }
+    } else {
+        float4 *o = reinterpret_cast<float4 *>((float *)gx + base);
+#pragma unroll
+        for (int i = 0; i < L / 4; i++) {
+            float v[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                v[j] = xh[4 * i + j] + xlo[4 * i + j];
+                finite = finite && isfinite(v[j]);
+            }
+            o[i] = make_float4(v[0], v[1], v[2], v[3]);
+        }
+    }
+    return finite;
+}
+
 }  // namespace tile
 }  // namespace tprgb
