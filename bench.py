@@ -251,10 +251,9 @@ def run_ours(args):
     worst_e2e, _ = port.batch_rel_l2(bt, xh.numpy(), truth)
 
     if dist:
-        t = torch.tensor([total_ms, e2e_s, worst, worst_e2e],
-                         dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms, e2e_s, worst, worst_e2e = t.tolist()
+        from tpr_gb300 import replicas
+        total_ms, e2e_s, worst, worst_e2e = replicas.aggregate(
+            [total_ms, e2e_s, worst, worst_e2e])
 
     ms_per_step = total_ms / args.steps
     value = world * NSYS / (ms_per_step * 1e-3)

@@ -139,10 +139,18 @@ struct Server {
         unsigned *h_ctl = nullptr;
         size_t cap_items = 0, cap_sys = 0, cap_large = 0;
     } buf[2];
-    long long *g_off = nullptr;   // generator tables (device)
-    int *g_n = nullptr;
-    unsigned long long *g_seed = nullptr;
-    size_t g_cap = 0;
+    // generator tables for seeded requests, double-buffered: pinned host
+    // staging + device copy; gen_ev[i] marks when table i may be reused
+    struct Gen {
+        long long *off = nullptr, *h_off = nullptr;
+        int *n = nullptr, *h_n = nullptr;
+        unsigned long long *seed = nullptr, *h_seed = nullptr;
+        size_t cap = 0;
+        cudaEvent_t ev = nullptr;
+        bool used = false;
+    } gen[2];
+    int gen_next = 0;
+    cudaEvent_t step_ev[4] = {nullptr, nullptr, nullptr, nullptr};
     int mode = 1, grid = 0;
 
     std::mutex mu;
@@ -193,43 +201,74 @@ static int ensure_buf(Server *s, Server::Buf &b, size_t nitems, size_t nsys,
     return TPRGB_OK;
 }
 
-// Upload / generate an admitted request's systems into its range.
-static int prepare(Server *s, Request &r) {
+// Upload an admitted host-array request into its range (async).
+static int prepare_host(Server *s, Request &r) {
     const long long at = r.at;
-    if (r.ha) {
-        size_t bytes = sizeof(float) * (size_t)r.neq;
-        TPRGB_CUDA(cudaMemcpyAsync(s->A + at, r.ha, bytes, cudaMemcpyHostToDevice, s->prep));
-        TPRGB_CUDA(cudaMemcpyAsync(s->B + at, r.hb, bytes, cudaMemcpyHostToDevice, s->prep));
-        TPRGB_CUDA(cudaMemcpyAsync(s->Cc + at, r.hc, bytes, cudaMemcpyHostToDevice, s->prep));
-        TPRGB_CUDA(cudaMemcpyAsync(s->D + at, r.hd, bytes, cudaMemcpyHostToDevice, s->prep));
-        return TPRGB_OK;
-    }
-    // seeded: small tables, then the generator kernel
-    if ((size_t)r.nsys > s->g_cap) {
-        TPRGB_CUDA(cudaStreamSynchronize(s->prep));
-        cudaFree(s->g_off);
-        cudaFree(s->g_n);
-        cudaFree(s->g_seed);
-        size_t c = std::max<size_t>(r.nsys, 1024);
-        TPRGB_CUDA(cudaMalloc(&s->g_off, sizeof(long long) * c));
-        TPRGB_CUDA(cudaMalloc(&s->g_n, sizeof(int) * c));
-        TPRGB_CUDA(cudaMalloc(&s->g_seed, sizeof(unsigned long long) * c));
-        s->g_cap = c;
-    }
-    std::vector<long long> off(r.nsys);
-    for (int k = 0; k < r.nsys; k++) off[k] = at + r.rel[k];
-    // the tables are reused by the next request: wait for this copy
-    TPRGB_CUDA(cudaMemcpyAsync(s->g_off, off.data(), sizeof(long long) * r.nsys,
-                               cudaMemcpyHostToDevice, s->prep));
-    TPRGB_CUDA(cudaMemcpyAsync(s->g_n, r.ns.data(), sizeof(int) * r.nsys,
-                               cudaMemcpyHostToDevice, s->prep));
-    TPRGB_CUDA(cudaMemcpyAsync(s->g_seed, r.seeds.data(),
-                               sizeof(unsigned long long) * r.nsys,
-                               cudaMemcpyHostToDevice, s->prep));
-    int rc = launch_generate(r.nsys, s->g_off, s->g_n, s->g_seed, r.kind, s->A,
-                             s->B, s->Cc, s->D, s->prep);
+    size_t bytes = sizeof(float) * (size_t)r.neq;
+    TPRGB_CUDA(cudaMemcpyAsync(s->A + at, r.ha, bytes, cudaMemcpyHostToDevice, s->prep));
+    TPRGB_CUDA(cudaMemcpyAsync(s->B + at, r.hb, bytes, cudaMemcpyHostToDevice, s->prep));
+    TPRGB_CUDA(cudaMemcpyAsync(s->Cc + at, r.hc, bytes, cudaMemcpyHostToDevice, s->prep));
+    TPRGB_CUDA(cudaMemcpyAsync(s->D + at, r.hd, bytes, cudaMemcpyHostToDevice, s->prep));
+    return TPRGB_OK;
+}
+
+static int gen_reserve(Server::Gen &g, size_t nsys) {
+    if (nsys <= g.cap) return TPRGB_OK;
+    if (g.used) TPRGB_CUDA(cudaEventSynchronize(g.ev));
+    cudaFree(g.off);
+    cudaFree(g.n);
+    cudaFree(g.seed);
+    cudaFreeHost(g.h_off);
+    cudaFreeHost(g.h_n);
+    cudaFreeHost(g.h_seed);
+    size_t c = std::max(nsys, 2 * g.cap);
+    TPRGB_CUDA(cudaMalloc(&g.off, sizeof(long long) * c));
+    TPRGB_CUDA(cudaMalloc(&g.n, sizeof(int) * c));
+    TPRGB_CUDA(cudaMalloc(&g.seed, sizeof(unsigned long long) * c));
+    TPRGB_CUDA(cudaHostAlloc(&g.h_off, sizeof(long long) * c, 0));
+    TPRGB_CUDA(cudaHostAlloc(&g.h_n, sizeof(int) * c, 0));
+    TPRGB_CUDA(cudaHostAlloc(&g.h_seed, sizeof(unsigned long long) * c, 0));
+    g.cap = c;
+    return TPRGB_OK;
+}
+
+// Generate every seeded request admitted in this round with one table
+// upload and one generator launch on the preparation stream.
+static int prepare_seeded(Server *s, std::vector<Request *> &rs) {
+    size_t total = 0;
+    for (Request *r : rs) total += (size_t)r->nsys;
+    if (!total) return TPRGB_OK;
+    Server::Gen &g = s->gen[s->gen_next];
+    s->gen_next ^= 1;
+    if (g.used) TPRGB_CUDA(cudaEventSynchronize(g.ev));  // table free again
+    int rc = gen_reserve(g, total);
     if (rc) return rc;
-    TPRGB_CUDA(cudaStreamSynchronize(s->prep));
+    size_t k = 0;
+    for (Request *r : rs)
+        for (int j = 0; j < r->nsys; j++, k++) {
+            g.h_off[k] = r->at + r->rel[j];
+            g.h_n[k] = r->ns[j];
+            g.h_seed[k] = r->seeds[j];
+        }
+    TPRGB_CUDA(cudaMemcpyAsync(g.off, g.h_off, sizeof(long long) * total,
+                               cudaMemcpyHostToDevice, s->prep));
+    TPRGB_CUDA(cudaMemcpyAsync(g.n, g.h_n, sizeof(int) * total,
+                               cudaMemcpyHostToDevice, s->prep));
+    TPRGB_CUDA(cudaMemcpyAsync(g.seed, g.h_seed, sizeof(unsigned long long) * total,
+                               cudaMemcpyHostToDevice, s->prep));
+    // one generator launch per run of consecutive requests of one kind
+    size_t b = 0;
+    for (size_t i = 0; i < rs.size();) {
+        size_t j = i, e = b;
+        while (j < rs.size() && rs[j]->kind == rs[i]->kind) e += (size_t)rs[j++]->nsys;
+        rc = launch_generate((int)(e - b), g.off + b, g.n + b, g.seed + b,
+                             rs[i]->kind, s->A, s->B, s->Cc, s->D, s->prep);
+        if (rc) return rc;
+        b = e;
+        i = j;
+    }
+    TPRGB_CUDA(cudaEventRecord(g.ev, s->prep));
+    g.used = true;
     return TPRGB_OK;
 }
 
@@ -291,7 +330,7 @@ static int launch_step(Server *s) {
             TPRGB_CUDA(cudaMemcpyAsync(rp->hx, s->X + rp->at,
                                        sizeof(double) * (size_t)rp->neq,
                                        cudaMemcpyDeviceToHost, cs));
-    TPRGB_CUDA(cudaEventCreateWithFlags(&st.done, cudaEventDisableTiming));
+    st.done = s->step_ev[st.id & 3];
     TPRGB_CUDA(cudaEventRecord(st.done, cs));
     s->inflight.push_back(std::move(st));
     return TPRGB_OK;
@@ -321,7 +360,6 @@ static void finish_step(Server *s, Step &st) {
         s->eq_done += rp->neq;
     }
     s->steps++;
-    cudaEventDestroy(st.done);
 }
 
 static void scheduler(Server *s) {
@@ -335,28 +373,38 @@ static void scheduler(Server *s) {
             s->cv_done.notify_all();
         }
         // 2. admission (FIFO; stop at the first request that does not fit)
-        int admitted = 0;
+        std::vector<std::shared_ptr<Request>> adm;
         while (!s->pending.empty()) {
             auto r = s->pending.front();
             long long at = s->alloc->alloc(r->neq);
             if (at < 0) break;
             r->at = at;
             s->pending.pop_front();
-            lk.unlock();
-            int rc = prepare(s, *r);
-            lk.lock();
-            if (rc) {
-                r->state = 4;
-                r->status = rc;
-                r->t_done = Clock::now();
-                s->alloc->release(r->at, r->neq);
-                r->at = -1;
-                s->cv_done.notify_all();
-                continue;
+            adm.push_back(r);
+        }
+        if (!adm.empty()) {
+            std::vector<Request *> seeded;
+            int rc = TPRGB_OK;
+            for (auto &r : adm) {
+                if (r->ha)
+                    rc = rc ? rc : prepare_host(s, *r);
+                else
+                    seeded.push_back(r.get());
             }
-            r->state = 1;
-            s->ready.push_back(r);
-            admitted++;
+            if (!rc) rc = prepare_seeded(s, seeded);
+            for (auto &r : adm) {
+                if (rc) {
+                    r->state = 4;
+                    r->status = rc;
+                    r->t_done = Clock::now();
+                    s->alloc->release(r->at, r->neq);
+                    r->at = -1;
+                } else {
+                    r->state = 1;
+                    s->ready.push_back(r);
+                }
+            }
+            if (rc) s->cv_done.notify_all();
         }
         // 3. next step: keep at most two in flight
         if (!s->ready.empty() && s->inflight.size() < 2) {
@@ -374,10 +422,9 @@ static void scheduler(Server *s) {
             s->cv_work.wait_for(lk, std::chrono::milliseconds(2));
         } else {
             lk.unlock();
-            std::this_thread::sleep_for(std::chrono::microseconds(20));
+            std::this_thread::yield();
             lk.lock();
         }
-        (void)admitted;
     }
 }
 
@@ -389,7 +436,6 @@ static void server_free(Server *s) {
     }
     if (s->comp) cudaStreamSynchronize(s->comp);
     if (s->prep) cudaStreamSynchronize(s->prep);
-    for (auto &st : s->inflight) cudaEventDestroy(st.done);
     for (auto &b : s->buf) {
         cudaFree(b.items);
         cudaFree(b.off);
@@ -399,9 +445,17 @@ static void server_free(Server *s) {
         cudaFreeHost(b.h_off);
         cudaFreeHost(b.h_ctl);
     }
-    cudaFree(s->g_off);
-    cudaFree(s->g_n);
-    cudaFree(s->g_seed);
+    for (auto &g : s->gen) {
+        cudaFree(g.off);
+        cudaFree(g.n);
+        cudaFree(g.seed);
+        cudaFreeHost(g.h_off);
+        cudaFreeHost(g.h_n);
+        cudaFreeHost(g.h_seed);
+        if (g.ev) cudaEventDestroy(g.ev);
+    }
+    for (auto &e : s->step_ev)
+        if (e) cudaEventDestroy(e);
     cudaFree(s->A);
     for (int i = 0; i < 2; i++)
         if (s->prep_ev[i]) cudaEventDestroy(s->prep_ev[i]);
@@ -505,6 +559,18 @@ TPRGB_API int tprgb_server_create(const tprgb_server_opts *opts,
         cudaEventCreateWithFlags(&s->prep_ev[1], cudaEventDisableTiming) != cudaSuccess) {
         server_free(s);
         return fail(TPRGB_ECUDA, "server streams");
+    }
+    for (auto &e : s->step_ev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) rc = TPRGB_ECUDA;
+    for (auto &g : s->gen) {
+        if (cudaEventCreateWithFlags(&g.ev, cudaEventDisableTiming) != cudaSuccess) rc = TPRGB_ECUDA;
+        if (!rc) rc = gen_reserve(g, 1 << 16);
+    }
+    for (auto &b : s->buf)
+        if (!rc) rc = ensure_buf(s, b, 1 << 16, 1 << 16, 1 << 12);
+    if (rc) {
+        server_free(s);
+        return rc;
     }
     s->thr = std::thread(scheduler, s);
     *out = new tprgb_server{s};
