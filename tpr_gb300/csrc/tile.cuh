@@ -108,17 +108,29 @@ __device__ __forceinline__ void solve(const float (&a)[L], const float (&b)[L],
         __syncthreads();
         Row S0{0.f, 0.f, 0.f}, S1{0.f, 0.f, 0.f};
         const int q2 = lane & (W - 1);
-        if (w == 0) {
+        if (!pc.on) {
+            // every warp of the system solves the 2W segment rows itself:
+            // no idle warps and no second barrier (the rows buffer is
+            // rewritten only after a later barrier)
             if (lane < W) {
                 S0 = sm.rows[sys_warp0 + lane].R0;
                 S1 = sm.rows[sys_warp0 + lane].R1;
             }
             hier::seg_reduce_k<W>(S0, S1, q2);
-        }
-        float yf = 0.f, yl = 0.f;
-        if (!pc.on) {
-            if (w == 0) hier::seg_top_k<W>(S0, S1, yf, yl);
+            float yf, yl, y0, y1;
+            hier::seg_top_k<W>(S0, S1, yf, yl);
+            hier::seg_back(S0, S1, q2, W, yf, yl, y0, y1);
+            xf = __shfl_sync(0xffffffffu, y0, w, W);
+            xl = __shfl_sync(0xffffffffu, y1, w, W);
         } else {
+            float yf = 0.f, yl = 0.f;
+            if (w == 0) {
+                if (lane < W) {
+                    S0 = sm.rows[sys_warp0 + lane].R0;
+                    S1 = sm.rows[sys_warp0 + lane].R1;
+                }
+                hier::seg_reduce_k<W>(S0, S1, q2);
+            }
             // level 3: this CTA's two boundary rows -> scratch, barrier,
             // every part solves the 2P-row system redundantly
             const unsigned par = pc.round & 1u;
@@ -147,17 +159,15 @@ __device__ __forceinline__ void solve(const float (&a)[L], const float (&b)[L],
                 hier::seg_back(U0, U1, q3, P, zf, zl, z0, z1);
                 yf = __shfl_sync(0xffffffffu, z0, pc.p);
                 yl = __shfl_sync(0xffffffffu, z1, pc.p);
+                float y0, y1;
+                hier::seg_back(S0, S1, q2, W, yf, yl, y0, y1);
+                if (lane < W) sm.x[sys_warp0 + lane] = make_float2(y0, y1);
             }
+            __syncthreads();
+            float2 v = sm.x[warp];
+            xf = v.x;
+            xl = v.y;
         }
-        if (w == 0) {
-            float y0, y1;
-            hier::seg_back(S0, S1, q2, W, yf, yl, y0, y1);
-            if (lane < W) sm.x[sys_warp0 + lane] = make_float2(y0, y1);
-        }
-        __syncthreads();
-        float2 v = sm.x[warp];
-        xf = v.x;
-        xl = v.y;
     }
     float x0, x1;
     hier::seg_back(R0, R1, q, K, xf, xl, x0, x1);
@@ -193,7 +203,8 @@ __device__ __forceinline__ void neighbours(float hfirst, float hlast,
             hp = v.x;
             lp = v.y;
         }
-        __syncthreads();
+        // no second barrier: sm.edge is rewritten only in the next
+        // refinement step, after the correction solve's barriers
     }
     if (pc.on) {
         // neighbouring parts' edge values through scratch
