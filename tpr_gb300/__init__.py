@@ -50,6 +50,8 @@ def _declare(L):
         "tprgb_ref_solve_device": (i, [i, i, i, i, i, vp, vp, vp, vp, vp, sz,
                                        vp]),
         "tprgb_normalize_device": (i, [i, C.c_int64, vp, vp, vp, vp, vp]),
+        "tprgb_ref_solve_device_static": (i, [i, i, i, i, i, vp, vp, vp, vp,
+                                              vp]),
         "tprgb_create": (i, [i, i, i, i, C.POINTER(vp)]),
         "tprgb_destroy": (i, [vp]),
         "tprgb_set_system": (i, [vp, vp, vp, vp, vp]),

@@ -698,3 +698,78 @@ int launch_normalize(int prec, long long neq, void *a, const void *diag,
 }
 
 }  // namespace tprgb
+
+// ---- reference-semantics solve with a built-in workspace ---------------------
+// For callers that cannot allocate device memory: code running inside CUDA
+// stream capture (a cudaMalloc there is not captured and may synchronise),
+// latency-critical loops where an allocation would stall the device, and
+// host applications or plugins whose device memory is owned by another
+// allocator that forbids outside allocations.  The sliced path's workspace
+// (3n + 3n/s elements per system) lives in this file-scope array instead of
+// caller memory.  Every GPU that loads the library reserves it until the
+// process exits.
+#include <mutex>
+
+namespace tprgb {
+
+constexpr size_t kStaticWorkBytes = 16u << 20;  // 16 MiB
+static __device__ __align__(256) unsigned char g_static_work[kStaticWorkBytes];
+
+// Device address of g_static_work per device, looked up once per device
+// (with that device current) on the first call made on it.
+static std::mutex g_static_mu;
+static void *g_static_ptr[64];
+
+static int static_work_ptr(void **out) {
+    int dev = 0;
+    TPRGB_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(TPRGB_EUNSUPPORTED, "device %d", dev);
+    std::lock_guard<std::mutex> lk(g_static_mu);
+    if (!g_static_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_static_work);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_static_work)");
+        g_static_ptr[dev] = p;
+    }
+    *out = g_static_ptr[dev];
+    return TPRGB_OK;
+}
+
+}  // namespace tprgb
+
+// Same contract and results as tprgb_ref_solve_device, with the workspace
+// taken from the library's own 16 MiB device array instead of the caller:
+// nothing is allocated.  The first call on a device looks up the array's
+// device address (cudaGetSymbolAddress), so make that first call before any
+// stream capture.  Systems whose workspace exceeds 16 MiB in total
+// (nsys * (3n + 3n/s) elements) are rejected with TPRGB_EUNSUPPORTED.
+// All calls share the array (no part of it needs to start at zero: every
+// workspace element is written before it is read), so calls that overlap on
+// the GPU -- on different streams, or from different threads -- race; keep
+// them ordered on one stream.
+extern "C" TPRGB_API int tprgb_ref_solve_device_static(
+    int kind, int nsys, int n, int s, int prec, const void *d_a,
+    const void *d_c, const void *d_rhs, void *d_x, void *stream) {
+    using namespace tprgb;
+    int rc = ref_validate(kind, n, s, prec);
+    if (rc) return rc;
+    if (nsys < 0 || nsys > 65535)
+        return fail(TPRGB_EINVAL, "nsys=%d outside [0, 65535]", nsys);
+    if (nsys == 0) return TPRGB_OK;
+    if (!d_a || !d_c || !d_rhs || !d_x)
+        return fail(TPRGB_EINVAL, "null device pointer");
+    void *work = nullptr;
+    if (ref_needs_workspace(kind, n, s, prec)) {
+        const size_t esz = prec == TPRGB_F32 ? 4 : 8;
+        const size_t need = ref_workspace_elems(kind, n, s) * esz * (size_t)nsys;
+        if (need > kStaticWorkBytes)
+            return fail(TPRGB_EUNSUPPORTED,
+                        "workspace of %zu bytes exceeds the built-in %zu bytes "
+                        "(use tprgb_ref_solve_device with caller memory)",
+                        need, kStaticWorkBytes);
+        rc = static_work_ptr(&work);
+        if (rc) return rc;
+    }
+    return launch_ref(kind, nsys, n, s, prec, d_a, d_c, d_rhs, d_x,
+                      (long long)n, work, (cudaStream_t)stream);
+}
