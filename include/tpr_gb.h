@@ -117,7 +117,8 @@ TPRGB_API int tprgb_create(int kind, int n, int s, int prec,
 TPRGB_API int tprgb_destroy(tprgb_solver *h);
 
 /* set_tridiagonal_system: host arrays of n elements of the handle's type,
- * copied to the device.  diag == NULL is the 3-argument form (unit
+ * copied (through the handle's pinned staging) to the device; the caller
+ * may reuse its arrays as soon as this returns.  diag == NULL is the 3-argument form (unit
  * diagonal assumed); otherwise the system is normalised by diag on the
  * device, as the 4-argument form does.  The caller's arrays are not
  * modified (the reference divides them in place). */
@@ -125,8 +126,8 @@ TPRGB_API int tprgb_set_system(tprgb_solver *h, const void *a,
                                const void *diag, const void *c,
                                const void *rhs);
 
-/* solve(): runs on the handle's stream and waits for it; *flops (may be
- * NULL) receives the reference flop count. */
+/* solve(): enqueues the solve on the handle's stream; *flops (may be NULL)
+ * receives the reference flop count.  get_ans waits for it. */
 TPRGB_API int tprgb_solve(tprgb_solver *h, int *flops);
 
 /* get_ans(x): copies the n-element solution to host memory. */

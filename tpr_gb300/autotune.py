@@ -30,7 +30,8 @@ SIZES = [16, 32, 64, 128, 256, 512, 1024, 2048, 4096, 8192]
 # (equations per thread, threads per CTA, variant: 1 registers, 2 staged)
 CANDIDATES = [(4, 128, 1), (4, 256, 1), (4, 512, 1), (4, 1024, 1),
               (8, 128, 1), (8, 256, 1), (8, 512, 1), (8, 1024, 1),
-              (4, 256, 2), (4, 512, 2), (8, 256, 2), (8, 512, 2)]
+              (4, 128, 2), (4, 256, 2), (4, 512, 2),
+              (8, 128, 2), (8, 256, 2), (8, 512, 2)]
 
 
 def _device_name():

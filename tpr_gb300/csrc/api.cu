@@ -65,6 +65,10 @@ struct tprgb_solver {
     int kind, n, s, prec;
     size_t esz;
     void *d_a = nullptr, *d_c = nullptr, *d_r = nullptr, *d_diag = nullptr;
+    // pinned staging (a, c, rhs, diag | x) so one solve costs one host
+    // synchronisation (in get_ans)
+    unsigned char *h_stage = nullptr, *h_x = nullptr;
+    cudaEvent_t staged = nullptr;  // the last upload has left h_stage
     void *d_x = nullptr, *d_work = nullptr;
     cudaStream_t stream = nullptr;
     bool has_system = false;
@@ -137,6 +141,8 @@ TPRGB_API int tprgb_normalize_device(int prec, int64_t neq, void *d_a,
 
 static void free_handle(tprgb_solver *h) {
     if (!h) return;
+    if (h->staged) cudaEventDestroy(h->staged);
+    cudaFreeHost(h->h_stage);
     cudaFree(h->d_a);
     cudaFree(h->d_work);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -167,6 +173,14 @@ TPRGB_API int tprgb_create(int kind, int n, int s, int prec,
         free_handle(h);
         return cuda_fail(e, "cudaMalloc(solver buffers)");
     }
+    e = cudaHostAlloc((void **)&h->h_stage, 5 * (size_t)n * h->esz, 0);
+    if (e == cudaSuccess)
+        e = cudaEventCreateWithFlags(&h->staged, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        free_handle(h);
+        return cuda_fail(e, "pinned staging");
+    }
+    h->h_x = h->h_stage + 4 * (size_t)n * h->esz;
     char *p = (char *)h->d_a;
     h->d_c = p + 1 * (size_t)n * h->esz;
     h->d_r = p + 2 * (size_t)n * h->esz;
@@ -195,21 +209,24 @@ TPRGB_API int tprgb_set_system(tprgb_solver *h, const void *a,
                                const void *rhs) {
     if (!h) return fail(TPRGB_EINVAL, "handle is NULL");
     if (!a || !c || !rhs) return fail(TPRGB_EINVAL, "null host array");
-    size_t bytes = (size_t)h->n * h->esz;
-    TPRGB_CUDA(cudaMemcpyAsync(h->d_a, a, bytes, cudaMemcpyHostToDevice, h->stream));
-    TPRGB_CUDA(cudaMemcpyAsync(h->d_c, c, bytes, cudaMemcpyHostToDevice, h->stream));
-    TPRGB_CUDA(cudaMemcpyAsync(h->d_r, rhs, bytes, cudaMemcpyHostToDevice, h->stream));
+    const size_t bytes = (size_t)h->n * h->esz;
+    // the previous upload must have left the staging buffer
+    TPRGB_CUDA(cudaEventSynchronize(h->staged));
     // CR ignores diag as the reference's setter does (src/cr.cpp:17-21)
-    if (diag && h->kind != TPRGB_CR) {
-        TPRGB_CUDA(cudaMemcpyAsync(h->d_diag, diag, bytes,
-                                   cudaMemcpyHostToDevice, h->stream));
+    const bool use_diag = diag && h->kind != TPRGB_CR;
+    memcpy(h->h_stage, a, bytes);
+    memcpy(h->h_stage + bytes, c, bytes);
+    memcpy(h->h_stage + 2 * bytes, rhs, bytes);
+    if (use_diag) memcpy(h->h_stage + 3 * bytes, diag, bytes);
+    // device layout a, c, rhs, diag is contiguous: one copy
+    TPRGB_CUDA(cudaMemcpyAsync(h->d_a, h->h_stage, (use_diag ? 4 : 3) * bytes,
+                               cudaMemcpyHostToDevice, h->stream));
+    TPRGB_CUDA(cudaEventRecord(h->staged, h->stream));
+    if (use_diag) {
         int rc = launch_normalize(h->prec, h->n, h->d_a, h->d_diag, h->d_c,
                                   h->d_r, h->stream);
         if (rc) return rc;
     }
-    // pageable sources: make the copies complete before the caller may
-    // reuse its arrays
-    TPRGB_CUDA(cudaStreamSynchronize(h->stream));
     h->has_system = true;
     return TPRGB_OK;
 }
@@ -218,10 +235,10 @@ TPRGB_API int tprgb_solve(tprgb_solver *h, int *flops) {
     if (!h) return fail(TPRGB_EINVAL, "handle is NULL");
     if (!h->has_system)
         return fail(TPRGB_EINVAL, "set_tridiagonal_system was not called");
+    // enqueued only: get_ans waits for it (and reports a failed launch)
     int rc = launch_ref(h->kind, 1, h->n, h->s, h->prec, h->d_a, h->d_c,
                         h->d_r, h->d_x, h->n, h->d_work, h->stream);
     if (rc) return rc;
-    TPRGB_CUDA(cudaStreamSynchronize(h->stream));
     if (flops) *flops = flops_of(h->kind, h->n, h->s);
     return TPRGB_OK;
 }
@@ -229,9 +246,11 @@ TPRGB_API int tprgb_solve(tprgb_solver *h, int *flops) {
 TPRGB_API int tprgb_get_ans(tprgb_solver *h, void *x) {
     if (!h) return fail(TPRGB_EINVAL, "handle is NULL");
     if (!x) return fail(TPRGB_EINVAL, "x is NULL");
-    TPRGB_CUDA(cudaMemcpyAsync(x, h->d_x, (size_t)h->n * h->esz,
-                               cudaMemcpyDeviceToHost, h->stream));
+    const size_t bytes = (size_t)h->n * h->esz;
+    TPRGB_CUDA(cudaMemcpyAsync(h->h_x, h->d_x, bytes, cudaMemcpyDeviceToHost,
+                               h->stream));
     TPRGB_CUDA(cudaStreamSynchronize(h->stream));
+    memcpy(x, h->h_x, bytes);
     return TPRGB_OK;
 }
 

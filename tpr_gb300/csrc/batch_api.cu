@@ -46,8 +46,8 @@ TPRGB_API int tprgb_tune_set(int n, int eq_per_thread, int threads_per_cta,
                              int variant) {
     if (variant < 0 || variant > 2) return fail(TPRGB_EINVAL, "variant %d", variant);
     TileConfig c{eq_per_thread, threads_per_cta, variant == 2 ? 1 : 0};
-    if (c.staged && c.nt != 256 && c.nt != 512)
-        return fail(TPRGB_EINVAL, "staged tiles use 256 or 512 threads");
+    if (c.staged && c.nt != 128 && c.nt != 256 && c.nt != 512)
+        return fail(TPRGB_EINVAL, "staged tiles use 128, 256 or 512 threads");
     int rc = batch_config_check(n, c);
     if (rc) return rc;
     int k = ilog2(n);
@@ -100,13 +100,13 @@ TPRGB_API int tprgb_batch_solve(int nsys, int n, const float *d_a,
     if (o.variant) cfg.staged = o.variant == 2 ? 1 : 0;
     BatchArgs A{d_a, d_b, d_c, d_d, d_x, nsys, n, o.refine_steps, o.residual,
                 o.x_f64};
-    const bool staged_ok = (cfg.nt == 256 || cfg.nt == 512) &&
+    const bool staged_ok = (cfg.nt == 128 || cfg.nt == 256 || cfg.nt == 512) &&
                            !(o.residual == TPRGB_RESID_F64 && o.refine_steps > 0);
     if (cfg.staged && staged_ok)
         return launch_batch_tma(A, cfg, (cudaStream_t)stream);
     if (o.variant == 2)
         return fail(TPRGB_EUNSUPPORTED,
-                    "staged kernel needs 256/512 threads and the compensated residual");
+                    "staged kernel needs 128/256/512 threads and the compensated residual");
     return launch_batch_uniform(A, cfg, (cudaStream_t)stream);
 }
 

@@ -24,7 +24,7 @@ namespace bt {
 constexpr unsigned kWaitLimit = 1u << 22;  // polls (~0.3 s with back-off)
 
 template <int L, int NT, int T, int MODE>
-__global__ void __launch_bounds__(NT, (NT <= 256 ? 3 : (NT <= 512 ? 1 : 1)))
+__global__ void __launch_bounds__(NT, (NT <= 128 ? 6 : (NT <= 256 ? 3 : 1)))
 batch_tma(const float *__restrict__ ga, const float *__restrict__ gb,
           const float *__restrict__ gc, const float *__restrict__ gd,
           void *__restrict__ gx, int nsys, int refine_steps, int x_f64) {
@@ -150,17 +150,20 @@ static int launch_tma_T(const BatchArgs &A, cudaStream_t st) {
 }
 
 // TMA-staged uniform batch (FP64 residual mode not provided: use the
-// register kernel).  Tiles: L in {4, 8}, nt in {256, 512}.
+// register kernel).  Tiles: L in {4, 8}, nt in {128, 256, 512}.
 int launch_batch_tma(const BatchArgs &A, const TileConfig &cfg, cudaStream_t st) {
     int rc = batch_config_check(A.n, cfg);
     if (rc) return rc;
     if (A.residual == TPRGB_RESID_F64 && A.refine_steps > 0)
         return fail(TPRGB_EUNSUPPORTED, "staged kernel has no FP64 residual mode");
-    if (cfg.nt != 256 && cfg.nt != 512)
-        return fail(TPRGB_EINVAL, "staged kernel tiles use 256 or 512 threads");
+    if (cfg.nt != 128 && cfg.nt != 256 && cfg.nt != 512)
+        return fail(TPRGB_EINVAL, "staged kernel tiles use 128, 256 or 512 threads");
     if (A.nsys == 0) return TPRGB_OK;
-    if (cfg.L == 4)
+    if (cfg.L == 4) {
+        if (cfg.nt == 128) return launch_tma_T<4, 128>(A, st);
         return cfg.nt == 256 ? launch_tma_T<4, 256>(A, st) : launch_tma_T<4, 512>(A, st);
+    }
+    if (cfg.nt == 128) return launch_tma_T<8, 128>(A, st);
     return cfg.nt == 256 ? launch_tma_T<8, 256>(A, st) : launch_tma_T<8, 512>(A, st);
 }
 

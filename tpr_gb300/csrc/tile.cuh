@@ -120,8 +120,10 @@ __device__ __forceinline__ void solve(const float (&a)[L], const float (&b)[L],
             float yf, yl, y0, y1;
             hier::seg_top_k<W>(S0, S1, yf, yl);
             hier::seg_back(S0, S1, q2, W, yf, yl, y0, y1);
-            xf = __shfl_sync(0xffffffffu, y0, w, W);
-            xl = __shfl_sync(0xffffffffu, y1, w, W);
+            // the rows sit in lanes 0..W-1 only: read lane w of the whole
+            // warp (a width-W shuffle would read other, empty segments)
+            xf = __shfl_sync(0xffffffffu, y0, w);
+            xl = __shfl_sync(0xffffffffu, y1, w);
         } else {
             float yf = 0.f, yl = 0.f;
             if (w == 0) {
