@@ -291,6 +291,9 @@ typedef struct tprgb_server_opts {
     int refine_steps;    /* default 1                                      */
     int residual;        /* TPRGB_RESID_DF (default) or TPRGB_RESID_F64     */
     int threads_per_cta; /* 256 (default) or 512                           */
+    long long max_step_eq; /* equations per step (0 = no cap); a larger
+                              request is solved over several steps, so an
+                              arrival never waits behind an unbounded step */
 } tprgb_server_opts;
 
 typedef struct tprgb_request_info {

@@ -90,6 +90,8 @@ plan_persistent(const float *__restrict__ ga, const float *__restrict__ gb,
         pc.round = 0;
         pc.status = status;
         pc.item = it;
+        pc.nsolve = 0;
+        pc.nb_hm = pc.nb_lm = pc.nb_hp = pc.nb_lp = 0.f;
         int T, t, sys;
         bool active, first_eq, last_eq;
         long long base;

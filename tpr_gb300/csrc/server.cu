@@ -17,6 +17,7 @@
 // Per-request latency = completion of its step (event) - submission.
 #include <algorithm>
 #include <atomic>
+#include <climits>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -106,14 +107,22 @@ struct Request {
     int state = 0;  // 0 pending, 1 admitted, 2 in step, 3 done, 4 failed
     int status = TPRGB_OK;
     unsigned nonfinite = 0;
-    long long step = -1;
+    long long step = -1;     // the step that solved its last system
+    int next_sys = 0;        // first system not yet given to a step
+    int unfinished = 0;      // systems given to steps and not yet solved
+    int timed_out = 0;
 };
 
 struct Step {
     long long id;
-    std::vector<std::shared_ptr<Request>> reqs;
-    std::vector<int> order;  // sorted system -> (req, sys) flattened index
-    std::vector<std::pair<int, int>> owner;
+    // systems [first, first + count) of each request in this step
+    struct Part {
+        std::shared_ptr<Request> req;
+        int first, count;
+    };
+    std::vector<Part> parts;
+    std::vector<int> order;  // sorted system -> flattened index
+    std::vector<int> owner;  // flattened index -> entry of parts
     int nsys = 0;
     cudaEvent_t done = nullptr;
     int buf = 0;
@@ -276,19 +285,39 @@ static int prepare_seeded(Server *s, std::vector<Request *> &rs) {
 static int launch_step(Server *s) {
     Step st;
     st.id = s->next_step++;
-    st.reqs.swap(s->ready);
     std::vector<int64_t> off;
     std::vector<int> ns;
-    for (int q = 0; q < (int)st.reqs.size(); q++) {
-        Request &r = *st.reqs[q];
-        r.state = 2;
-        r.step = st.id;
-        for (int k = 0; k < r.nsys; k++) {
+    // whole systems from the ready requests in FIFO order, up to the step's
+    // equation cap (a request larger than the cap spans several steps; the
+    // first system is always taken so every step makes progress)
+    const long long cap = s->o.max_step_eq > 0 ? s->o.max_step_eq : LLONG_MAX;
+    long long eq = 0;
+    size_t keep_from = 0;
+    for (size_t q = 0; q < s->ready.size(); q++) {
+        auto &rp = s->ready[q];
+        Request &r = *rp;
+        const int first = r.next_sys;
+        int k = first;
+        while (k < r.nsys && (eq == 0 || eq + r.ns[k] <= cap)) {
             off.push_back(r.at + r.rel[k]);
             ns.push_back(r.ns[k]);
-            st.owner.emplace_back(q, k);
+            st.owner.push_back((int)st.parts.size());
+            eq += r.ns[k];
+            k++;
         }
+        if (k > first) {
+            st.parts.push_back(Step::Part{rp, first, k - first});
+            r.next_sys = k;
+            r.unfinished += k - first;
+            r.state = 2;
+        }
+        if (r.next_sys < r.nsys) {  // cap reached inside this request
+            keep_from = q;
+            break;
+        }
+        keep_from = q + 1;
     }
+    s->ready.erase(s->ready.begin(), s->ready.begin() + keep_from);
     st.nsys = (int)ns.size();
     std::vector<int4> items;
     std::vector<long long> soff;
@@ -324,12 +353,17 @@ static int launch_step(Server *s) {
     // per-system status back to the pinned copy (read after completion)
     TPRGB_CUDA(cudaMemcpyAsync(b.h_ctl, b.ctl, sizeof(unsigned) * ctl_words,
                                cudaMemcpyDeviceToHost, cs));
-    // host-array requests: solution back to the caller
-    for (auto &rp : st.reqs)
-        if (rp->hx)
-            TPRGB_CUDA(cudaMemcpyAsync(rp->hx, s->X + rp->at,
-                                       sizeof(double) * (size_t)rp->neq,
-                                       cudaMemcpyDeviceToHost, cs));
+    // host-array requests: solved systems back to the caller
+    for (auto &pt : st.parts) {
+        Request &r = *pt.req;
+        if (!r.hx) continue;
+        const long long a0 = r.rel[pt.first];
+        const long long a1 = pt.first + pt.count < r.nsys ? r.rel[pt.first + pt.count]
+                                                          : r.neq;
+        TPRGB_CUDA(cudaMemcpyAsync(r.hx + a0, s->X + r.at + a0,
+                                   sizeof(double) * (size_t)(a1 - a0),
+                                   cudaMemcpyDeviceToHost, cs));
+    }
     st.done = s->step_ev[st.id & 3];
     TPRGB_CUDA(cudaEventRecord(st.done, cs));
     s->inflight.push_back(std::move(st));
@@ -341,23 +375,24 @@ static void finish_step(Server *s, Step &st) {
     const unsigned code = b.h_ctl[4];
     const unsigned nlarge = b.h_ctl[1] - 16;
     auto now = Clock::now();
-    for (int k = 0; k < st.nsys; k++) {
-        const unsigned v = b.h_ctl[16 + nlarge + k];
-        if (v) {
-            auto ow = st.owner[st.order[k]];
-            st.reqs[ow.first]->nonfinite++;
+    for (int k = 0; k < st.nsys; k++)
+        if (b.h_ctl[16 + nlarge + k]) st.parts[st.owner[st.order[k]]].req->nonfinite++;
+    for (auto &pt : st.parts) {
+        Request &r = *pt.req;
+        if (code == TPRGB_ETIMEOUT) r.timed_out = 1;
+        r.unfinished -= pt.count;
+        s->systems_done += pt.count;
+        if (r.unfinished == 0 && r.next_sys == r.nsys) {
+            r.t_done = now;
+            r.state = 3;
+            r.step = st.id;
+            if (r.timed_out)
+                r.status = TPRGB_ETIMEOUT;
+            else if (r.nonfinite)
+                r.status = TPRGB_ENONFINITE;
+            s->requests_done++;
+            s->eq_done += r.neq;
         }
-    }
-    for (auto &rp : st.reqs) {
-        rp->t_done = now;
-        rp->state = 3;
-        if (code == TPRGB_ETIMEOUT)
-            rp->status = TPRGB_ETIMEOUT;
-        else if (rp->nonfinite)
-            rp->status = TPRGB_ENONFINITE;
-        s->requests_done++;
-        s->systems_done += rp->nsys;
-        s->eq_done += rp->neq;
     }
     s->steps++;
 }
@@ -412,7 +447,7 @@ static void scheduler(Server *s) {
             if (rc) {
                 s->fatal = rc;
                 for (auto &st : s->inflight)
-                    for (auto &rp : st.reqs) rp->state = 4, rp->status = rc;
+                    for (auto &pt : st.parts) pt.req->state = 4, pt.req->status = rc;
                 s->cv_done.notify_all();
                 break;
             }
@@ -517,6 +552,7 @@ TPRGB_API int tprgb_server_opts_default(tprgb_server_opts *o) {
     o->refine_steps = 1;
     o->residual = TPRGB_RESID_DF;
     o->threads_per_cta = 256;
+    o->max_step_eq = 0;
     return TPRGB_OK;
 }
 

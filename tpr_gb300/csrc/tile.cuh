@@ -25,7 +25,7 @@ struct Smem {
     SegRows rows[NT / 32];
     float2 x[NT / 32];
     float4 edge[2 * (NT / 32)];
-    float2 part_x;  // this part's first / last unknown (multi-CTA systems)
+    float2 part_nb;  // previous part's last / next part's first unknown
     int ok;
 };
 
@@ -38,6 +38,12 @@ struct Part {
     unsigned round;
     DeviceStatus *status;
     int item;
+    // neighbouring parts' edge unknowns as (hi, lo) pairs, taken from the
+    // level-3 solution every part computes: nb_hm/nb_lm = previous part's
+    // last, nb_hp/nb_lp = next part's first.  Solve 0 sets hi, corrections
+    // accumulate into lo.
+    int nsolve;
+    float nb_hm, nb_lm, nb_hp, nb_lp;
 };
 
 constexpr int kScratchFloats = 4 + 2 * 32 * 8 + 2 * 32 * 4;  // per system
@@ -51,9 +57,12 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
 // Barrier between the CTAs holding the parts of one system.  Bounded: on
 // timeout it records TPRGB_ETIMEOUT and returns false (results of that
 // system are then invalid, the kernel still finishes).
+// Threads that wrote scratch for this round fence their writes themselves
+// (writer_fence) before the barrier; the others need no fence.
+__device__ __forceinline__ void writer_fence() { __threadfence(); }
+
 template <int NT>
 __device__ bool part_barrier(Part &pc, Smem<NT> &sm, int where) {
-    __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
         atomicAdd(pc.counter, 1u);
@@ -139,10 +148,12 @@ __device__ __forceinline__ void solve(const float (&a)[L], const float (&b)[L],
             if (warp == 0 && lane == 0) {
                 float4 *dst = reinterpret_cast<float4 *>(pc.rows + (par * 32 + pc.p) * 8);
                 __stcg(dst, make_float4(S0.a, S0.c, S0.d, 0.f));
+                writer_fence();
             }
             if (warp == 0 && lane == W - 1) {
                 float4 *dst = reinterpret_cast<float4 *>(pc.rows + (par * 32 + pc.p) * 8 + 4);
                 __stcg(dst, make_float4(S1.a, S1.c, S1.d, 0.f));
+                writer_fence();
             }
             part_barrier<NT>(pc, sm, 1);
             if (warp == 0) {
@@ -161,6 +172,13 @@ __device__ __forceinline__ void solve(const float (&a)[L], const float (&b)[L],
                 hier::seg_back(U0, U1, q3, P, zf, zl, z0, z1);
                 yf = __shfl_sync(0xffffffffu, z0, pc.p);
                 yl = __shfl_sync(0xffffffffu, z1, pc.p);
+                // neighbours' edge unknowns for the next residual: no
+                // separate exchange needed
+                const float pl = __shfl_sync(0xffffffffu, z1, pc.p > 0 ? pc.p - 1 : 0);
+                const float nf = __shfl_sync(0xffffffffu, z0, pc.p < P - 1 ? pc.p + 1 : 0);
+                if (lane == 0)
+                    sm.part_nb = make_float2(pc.p > 0 ? pl : 0.f,
+                                             pc.p < P - 1 ? nf : 0.f);
                 float y0, y1;
                 hier::seg_back(S0, S1, q2, W, yf, yl, y0, y1);
                 if (lane < W) sm.x[sys_warp0 + lane] = make_float2(y0, y1);
@@ -169,6 +187,17 @@ __device__ __forceinline__ void solve(const float (&a)[L], const float (&b)[L],
             float2 v = sm.x[warp];
             xf = v.x;
             xl = v.y;
+            const float2 nb = sm.part_nb;
+            if (pc.nsolve == 0) {
+                pc.nb_hm = nb.x;
+                pc.nb_lm = 0.f;
+                pc.nb_hp = nb.y;
+                pc.nb_lp = 0.f;
+            } else {
+                pc.nb_lm += nb.x;
+                pc.nb_lp += nb.y;
+            }
+            pc.nsolve++;
         }
     }
     float x0, x1;
@@ -209,33 +238,14 @@ __device__ __forceinline__ void neighbours(float hfirst, float hlast,
         // refinement step, after the correction solve's barriers
     }
     if (pc.on) {
-        // neighbouring parts' edge values through scratch
-        const unsigned par = pc.round & 1u;
-        float2 *mine = reinterpret_cast<float2 *>(pc.edges + (par * 32 + pc.p) * 4);
-        if (t == 0) __stcg(mine, make_float2(hfirst, lfirst));
-        if (t == T - 1) __stcg(mine + 1, make_float2(hlast, llast));
-        part_barrier<NT>(pc, sm, 2);
+        // neighbouring parts' edge values from the level-3 solutions
         if (t == 0) {
-            if (pc.p > 0) {
-                float4 v = __ldcg(reinterpret_cast<const float4 *>(
-                    pc.edges + (par * 32 + pc.p - 1) * 4));
-                hm = v.z;
-                lm = v.w;
-            } else {
-                hm = 0.f;
-                lm = 0.f;
-            }
+            hm = pc.nb_hm;
+            lm = pc.nb_lm;
         }
         if (t == T - 1) {
-            if (pc.p < pc.P - 1) {
-                float4 v = __ldcg(reinterpret_cast<const float4 *>(
-                    pc.edges + (par * 32 + pc.p + 1) * 4));
-                hp = v.x;
-                lp = v.y;
-            } else {
-                hp = 0.f;
-                lp = 0.f;
-            }
+            hp = pc.nb_hp;
+            lp = pc.nb_lp;
         }
     } else {
         if (t == 0) {

@@ -20,11 +20,13 @@ from .server import Server
 
 
 def run(nreq: int, budget_gib: float = 8.0, loads=(0.25, 0.5, 0.9),
-        seed: int = 11, max_sys: int = 512):
+        seed: int = 11, max_sys: int = 512, max_step_eq: int = 0):
     out = {"workload": f"{nreq} requests, U{{1..{max_sys}}} systems of "
                        f"N=2^U{{8..14}}, FP32 + 1 refinement, "
-                       f"{budget_gib:g} GiB budget", "loads": []}
-    with Server(budget_bytes=int(budget_gib * (1 << 30))) as s:
+                       f"{budget_gib:g} GiB budget, step cap "
+                       f"{max_step_eq or 'none'} eq", "loads": []}
+    with Server(budget_bytes=int(budget_gib * (1 << 30)),
+                max_step_eq=max_step_eq) as s:
         s.run_load(min(nreq, 64), 0.0, seed=seed + 99, max_sys=max_sys)  # warm
         lat, el, nsys, rc = s.run_load(nreq, 0.0, seed=seed, max_sys=max_sys)
         sat_req = nreq / el
@@ -47,10 +49,12 @@ def main():
     p = argparse.ArgumentParser()
     p.add_argument("--requests", type=int, default=100000)
     p.add_argument("--budget-gib", type=float, default=8.0)
+    p.add_argument("--max-step-eq", type=int, default=0)
     a = p.parse_args()
     from . import autotune
     autotune.apply()
-    print(json.dumps(run(a.requests, a.budget_gib)), flush=True)
+    print(json.dumps(run(a.requests, a.budget_gib,
+                         max_step_eq=a.max_step_eq)), flush=True)
 
 
 if __name__ == "__main__":

@@ -19,7 +19,7 @@ from .devgen import KIND
 class ServerOpts(C.Structure):
     _fields_ = [("budget_bytes", C.c_size_t), ("max_pending", C.c_int),
                 ("refine_steps", C.c_int), ("residual", C.c_int),
-                ("threads_per_cta", C.c_int)]
+                ("threads_per_cta", C.c_int), ("max_step_eq", C.c_longlong)]
 
 
 class RequestInfo(C.Structure):
@@ -63,7 +63,7 @@ def _declare(L):
 class Server:
     def __init__(self, budget_bytes: int = 8 << 30, refine_steps: int = 1,
                  residual: int = 0, threads_per_cta: int = 256,
-                 max_pending: int = 1 << 20):
+                 max_pending: int = 1 << 20, max_step_eq: int = 0):
         L = load()
         _declare(L)
         o = ServerOpts()
@@ -73,6 +73,7 @@ class Server:
         o.residual = residual
         o.threads_per_cta = threads_per_cta
         o.max_pending = max_pending
+        o.max_step_eq = max_step_eq
         self._h = C.c_void_p()
         self._keep = {}
         check(L.tprgb_server_create(C.byref(o), C.byref(self._h)))
