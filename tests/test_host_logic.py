@@ -1,0 +1,104 @@
+"""Host-side logic that needs no GPU: tuning table, generators, fixture
+reader, CLI argument handling, replica partitioning edge cases."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from tests.conftest import GOLDEN
+from tpr_gb300 import autotune, devgen
+from tpr_gb300 import generate as G
+from tpr_gb300 import nstab, pm
+
+
+def test_tune_table_apply_and_get(lib, tmp_path):
+    from tpr_gb300 import batch as B
+    lib.tprgb_tune_clear()
+    assert B.tile_for(1024)[:2] == (8, 256)          # built-in default
+    doc = {"device": "TEST-GPU", "tiles": {
+        "1024": {"eq_per_thread": 4, "threads_per_cta": 512, "variant": 2},
+        "64": {"eq_per_thread": 8, "threads_per_cta": 128, "variant": 1}}}
+    p = tmp_path / "t.json"
+    p.write_text(json.dumps(doc))
+    assert autotune.apply(str(p), device_name="OTHER-GPU") == 0
+    assert autotune.apply(str(p), device_name="TEST-GPU") == 2
+    assert B.tile_for(1024) == (4, 512, 2)
+    assert B.tile_for(64) == (8, 128, 1)
+    lib.tprgb_tune_clear()
+    assert B.tile_for(1024)[:2] == (8, 256)
+
+
+def test_tune_set_rejects_bad_tiles(lib):
+    import tpr_gb300 as T
+    assert lib.tprgb_tune_set(1024, 3, 256, 1) == T.EINVAL      # L
+    assert lib.tprgb_tune_set(1024, 8, 64, 1) == T.EUNSUPPORTED  # T > nt
+    assert lib.tprgb_tune_set(1024, 8, 1024, 2) == T.EINVAL     # staged nt
+    assert lib.tprgb_tune_set(1000, 8, 256, 1) == T.EINVAL      # n
+
+
+def test_committed_table_is_valid():
+    path = autotune.TABLE
+    if not os.path.exists(path):
+        pytest.skip("no tuned table committed")
+    doc = json.load(open(path))
+    for n, ent in doc["tiles"].items():
+        n = int(n)
+        assert n & (n - 1) == 0
+        assert ent["eq_per_thread"] in (4, 8)
+        assert n // ent["eq_per_thread"] <= ent["threads_per_cta"]
+
+
+def test_generators_deterministic_and_dominant():
+    for kind in G.KINDS:
+        a1, b1, c1, d1, x1 = G.one_system(256, 9, kind)
+        a2, b2, c2, d2, x2 = G.one_system(256, 9, kind)
+        for u, v in ((a1, a2), (b1, b2), (c1, c2), (d1, d2), (x1, x2)):
+            np.testing.assert_array_equal(u, v)
+        assert a1[0] == 0 and c1[-1] == 0
+        assert np.all(np.abs(b1) > np.abs(a1) + np.abs(c1))
+    ns = G.uneven_sizes(1000, 6, 16, 1)
+    assert set(np.unique(ns)) <= {1 << k for k in range(6, 17)}
+    bt = G.batch([64, 128], 3)
+    assert bt.neq == 192 and list(bt.offsets) == [0, 64]
+
+
+def test_device_generator_mirror_properties():
+    for kind in ("dominant", "uneven", "weak"):
+        a, b, c, d = devgen.system(512, 1234, kind)
+        assert a.dtype == np.float32 and a[0] == 0 and c[-1] == 0
+        assert np.all(b > np.abs(a) + np.abs(c))
+        a2, *_ = devgen.system(512, 1234, kind)
+        np.testing.assert_array_equal(a, a2)
+        a3, *_ = devgen.system(512, 1235, kind)
+        assert not np.array_equal(a, a3)
+
+
+def test_nstab_reader_matches_bundled_bands(tmp_path):
+    z = np.load(os.path.join(GOLDEN, "nstab.npz"))
+    a, diag, c, rhs = z["eq18"]
+    n = len(a)
+    # write the band back in the reference's dense-row format
+    rows = []
+    for i in range(n):
+        row = np.zeros(n + 1)
+        if i > 0:
+            row[i - 1] = a[i]
+        row[i] = diag[i]
+        if i < n - 1:
+            row[i + 1] = c[i]
+        row[n] = rhs[i]
+        rows.append(",".join(repr(float(v)) for v in row))
+    f = tmp_path / "eq18.txt"
+    f.write_text("\n".join(rows) + "\n")
+    got = nstab.read_fixture(str(f), n)
+    for u, v in zip(got, (a, diag, c, rhs)):
+        np.testing.assert_array_equal(u, v)
+    assert nstab.norm(z["xt"], z["xt"]) == 0.0
+
+
+def test_pm_cli_usage_and_unknown_solver(capsys):
+    assert pm.main([]) == 1
+    assert "Usage" in capsys.readouterr().err
+    with pytest.raises(SystemExit):
+        pm.run(64, 8, 1, "lapack")
