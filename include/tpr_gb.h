@@ -176,11 +176,15 @@ typedef struct tprgb_batch_opts {
     int refine_steps;    /* 0: plain FP32 solve; k: k refinement steps      */
     int residual;        /* TPRGB_RESID_DF or TPRGB_RESID_F64               */
     int x_f64;           /* 1: x is double[neq]; 0: x is float[neq]         */
-    int eq_per_thread;   /* 0: tuned table; otherwise 4 or 8                */
-    int threads_per_cta; /* 0: tuned table; otherwise 128, 256, 512, 1024   */
+    int eq_per_thread;   /* 0: tuned table; otherwise 4, 8 (16: variants 3,4) */
+    int threads_per_cta; /* 0: tuned table; otherwise 64 .. 1024 (below)    */
     int variant;         /* 0: tuned table; 1: inputs loaded to registers;
                             2: inputs staged in shared memory by TMA bulk
-                               copies (persistent CTAs, 256 or 512 threads) */
+                               copies (persistent CTAs, 128/256/512
+                               threads); 3: staged by swizzled 2D tensor-map
+                               copies, two stages (8 or 16 equations per
+                               thread, 64/128/256 threads, n >= 32);
+                            4: as 3 with one stage                         */
 } tprgb_batch_opts;
 
 /* Defaults: 1 refinement step, compensated residual, FP64 x, tuned tile. */
@@ -216,8 +220,8 @@ TPRGB_API int tprgb_batch_solve_host(tprgb_host_ctx *ctx, int nsys, int n,
                                      const tprgb_batch_opts *opts);
 
 /* ---- tile table (filled by the autotuner, tpr_gb300/autotune.py) ------
- * Tile of the uniform kernel for systems of size n: equations per thread
- * (4 or 8) and threads per CTA.  Also gives the equations per thread the
+ * Tile of the uniform kernel for systems of size n: equations per thread,
+ * threads per CTA and variant (as in tprgb_batch_opts).  Also gives the equations per thread the
  * uneven-batch plans use for that size. */
 TPRGB_API int tprgb_tune_set(int n, int eq_per_thread, int threads_per_cta,
                              int variant);
@@ -294,6 +298,10 @@ typedef struct tprgb_server_opts {
     long long max_step_eq; /* equations per step (0 = no cap); a larger
                               request is solved over several steps, so an
                               arrival never waits behind an unbounded step */
+    int max_inflight;    /* steps queued on the device at once: 2 (default)
+                            overlaps building the next step with the running
+                            one; 1 makes an arrival wait for at most the
+                            running step                                    */
 } tprgb_server_opts;
 
 typedef struct tprgb_request_info {
@@ -303,6 +311,9 @@ typedef struct tprgb_request_info {
     double latency_us;     /* submission -> solution resident on the device */
     long long x_offset;    /* first equation of the request in the arena    */
     long long neq;         /* equations in the request                      */
+    double queue_us;       /* submission -> the step that finished it was
+                              enqueued (admission, waiting for a step slot) */
+    double step_us;        /* device time of that step                      */
 } tprgb_request_info;
 
 typedef struct tprgb_server_stats {
@@ -348,13 +359,16 @@ TPRGB_API int tprgb_server_get_stats(tprgb_server *srv,
 /* Load driver: submits nreq seeded requests with Poisson arrivals at
  * rate_per_s (<= 0: all at once), each with U{min_sys..max_sys} systems of
  * size 2^k, k ~ U{kmin..kmax}; waits for and releases them in order.
- * latencies_us[i] (may be NULL) receives each request's latency, *elapsed_s
- * first submission -> last completion, *systems_out the systems solved. */
+ * latencies_us[i] (may be NULL) receives each request's latency,
+ * detail_us[3i..3i+2] (may be NULL) its queue_us, step_us and equations,
+ * *elapsed_s first submission -> last completion, *systems_out the systems
+ * solved. */
 TPRGB_API int tprgb_server_run_load(tprgb_server *srv, int nreq,
                                     double rate_per_s, uint64_t seed,
                                     int min_sys, int max_sys, int kmin,
                                     int kmax, int kind, double *latencies_us,
-                                    double *elapsed_s, long long *systems_out);
+                                    double *detail_us, double *elapsed_s,
+                                    long long *systems_out);
 
 /* ---- diagnostics ------------------------------------------------------- */
 /* Status word of the TMA-staged batched kernel: *code = TPRGB_ETIMEOUT if a

@@ -4,6 +4,7 @@ with refinement <= 1e-9 (the accuracy target of the refined solver)."""
 import numpy as np
 import pytest
 
+import tpr_gb300 as T
 from tpr_gb300 import batch as B
 from tpr_gb300 import generate as G
 
@@ -114,3 +115,50 @@ def test_staged_kernel_matches_register_kernel(cuda, port, n, L, nt):
     code = ctypes.c_uint()
     assert B.load().tprgb_batch_status(ctypes.byref(code), 1) == 0
     assert code.value == 0
+
+
+@pytest.mark.parametrize("n", [32, 64, 256, 1024, 4096])
+@pytest.mark.parametrize("L,nt", [(8, 64), (8, 128), (8, 256), (16, 64),
+                                  (16, 128), (16, 256)])
+def test_swizzled_kernel(cuda, port, n, L, nt):
+    """Tensor-map staging with the 128-byte swizzle: with 8 equations per
+    thread the same bits as the register variant; with 16 the refined
+    solution meets 1e-9 and the plain one 1e-5; one and two stages agree
+    bit for bit; the batch ends in a partial tile."""
+    if n < 2 * L or n // L > nt:
+        pytest.skip("tile does not cover this size")
+    nsys = 3 * (nt * L // n) + 1
+    bt = G.uniform_batch(nsys, n, 57 + n, "uneven")
+    xs = B.solve_host(bt, refine_steps=1, eq_per_thread=L, threads_per_cta=nt,
+                      variant=B.SWIZZLED)
+    x1 = B.solve_host(bt, refine_steps=1, eq_per_thread=L, threads_per_cta=nt,
+                      variant=B.SWIZZLED_ONE)
+    np.testing.assert_array_equal(xs, x1)
+    if L == 8 and nt >= 128:
+        xr = B.solve_host(bt, refine_steps=1, eq_per_thread=L,
+                          threads_per_cta=nt, variant=B.REGISTERS)
+        np.testing.assert_array_equal(xs, xr)
+    worst, _ = _err(port, bt, xs)
+    assert worst <= 1e-9, worst
+    xp = B.solve_host(bt, refine_steps=0, x_f64=False, eq_per_thread=L,
+                      threads_per_cta=nt, variant=B.SWIZZLED)
+    worst, _ = _err(port, bt, xp)
+    assert worst <= 1e-5, worst
+    import ctypes
+    code = ctypes.c_uint()
+    assert B.load().tprgb_batch_status(ctypes.byref(code), 1) == 0
+    assert code.value == 0
+
+
+def test_swizzled_rejects_bad_tiles(cuda):
+    bt = G.uniform_batch(4, 16, 3, "dominant")
+    with pytest.raises(T.TprError):   # n < 32
+        B.solve_host(bt, eq_per_thread=8, threads_per_cta=64,
+                     variant=B.SWIZZLED)
+    bt = G.uniform_batch(4, 64, 3, "dominant")
+    with pytest.raises(T.TprError):   # 512 threads
+        B.solve_host(bt, eq_per_thread=8, threads_per_cta=512,
+                     variant=B.SWIZZLED)
+    with pytest.raises(T.TprError):   # FP64 residual
+        B.solve_host(bt, eq_per_thread=8, threads_per_cta=64,
+                     variant=B.SWIZZLED, residual=B.RESID_F64)

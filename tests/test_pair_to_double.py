@@ -20,27 +20,16 @@ def emulate(hi, lo):
     s, e = _two_sum(np.float32(hi), np.float32(lo))
     u = int(np.array(s, np.float32).view(np.uint32))
     ex = (u >> 23) & 0xFF
-    if ex < 52 or ex == 255:
+    if ex < 53 or ex == 255:
         return float(s) + float(e)
     sign, mant = u & 0x80000000, u & 0x7FFFFF
     ue = int(np.array(e, np.float32).view(np.uint32))
-    ee = (ue >> 23) & 0xFF
-    k = 0
-    if ee != 0:
-        down = ((ue ^ u) & 0x80000000) != 0
-        m = (ue & 0x7FFFFF) | 0x800000
-        sh = ee - ex + 29 + (1 if (mant == 0 and down) else 0)
-        if sh >= 0:
-            kk = m << sh
-        elif sh > -25:
-            r = -sh
-            kk = m >> r
-            rem, half = m & ((1 << r) - 1), 1 << (r - 1)
-            if rem > half or (rem == half and (kk & 1)):
-                kk += 1
-        else:
-            kk = 0
-        k = -kk if down else kk
+    down = e != 0 and ((ue ^ u) & 0x80000000) != 0
+    sc = 306 - ex + (1 if (mant == 0 and down) else 0)
+    scale = np.array(sc << 23, np.uint32).view(np.float32)
+    prod = np.float32(np.float32(abs(e)) * scale)   # exact: a power of two
+    kk = int(np.rint(prod))                          # nearest, ties to even
+    k = -kk if down else kk
     bits = ((sign | ((ex + 896) << 20) | (mant >> 3)) << 32) | \
         ((mant & 7) << 29)
     bits = (bits + k) & ((1 << 64) - 1)
@@ -60,6 +49,15 @@ def cases(seed=0, n=20000):
                       0.0):
                 extra.append((np.float32(f * p), np.float32(f * p * r)))
     extra += [(0.0, 1e-30), (1e-40, 0.0), (3.0, 0.0), (1e-30, 1e-38)]
+    # smallest magnitudes on the integer route: subnormal low parts
+    for e in (-74, -73, -72):
+        for m in (1.0, 1.5, -1.0):
+            for t in (1e-45, -1e-45, 3e-39, -5.9e-39, 1.1e-38):
+                extra.append((np.float32(m * 2.0 ** e), np.float32(t)))
+    # largest magnitudes
+    for m in (3.4e38, -3.4e38, 2.0 ** 127, 1.7e38):
+        for r in (2.0 ** -25, -2.0 ** -26, 0.3 * 2.0 ** -24):
+            extra.append((np.float32(m), np.float32(m * r)))
     # exact halfway cases between doubles (ties to even)
     for h in (1.0, 1.0 + 2.0 ** -23, -1.0, 1.5, 2.0 ** 20):
         u = 2.0 ** (np.floor(np.log2(abs(h))) - 53)

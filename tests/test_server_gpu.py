@@ -140,4 +140,26 @@ def test_nonfinite_request_status(cuda):
 def test_load_driver_small(cuda):
     with Server(budget_bytes=1 << 30) as s:
         lat, el, nsys, rc = s.run_load(200, 2000.0, seed=4, max_sys=32)
+        det = s.last_detail
     assert rc == 0 and (lat > 0).all() and el > 0 and nsys >= 200
+    # queue time and the finishing step's device time both fit inside the
+    # latency; every request has equations
+    assert (det[:, 0] >= 0).all() and (det[:, 1] > 0).all()
+    assert (det[:, 0] + det[:, 1] <= lat + 50.0).all()
+    assert (det[:, 2] >= 256).all()
+
+
+def test_one_step_in_flight_same_bits(cuda):
+    rng = np.random.default_rng(21)
+    target = _req(rng, 12)
+    x_alone, _ = _solve_alone(*target)
+    with Server(budget_bytes=1 << 30, max_inflight=1) as s:
+        tickets = [s.submit_seeded(*_req(rng)) for _ in range(20)]
+        tt = s.submit_seeded(*target)
+        assert all(s.wait(t)["rc"] == 0 for t in tickets)
+        assert s.wait(tt)["rc"] == 0
+        np.testing.assert_array_equal(x_alone,
+                                      s.fetch(tt, int(target[0].sum())))
+    with pytest.raises(T.TprError) as e:
+        Server(budget_bytes=1 << 24, max_inflight=3)
+    assert e.value.code == T.EINVAL

@@ -27,11 +27,16 @@ from . import check, load
 PKG = os.path.dirname(os.path.abspath(__file__))
 TABLE = os.path.join(PKG, "tuned_tiles.json")
 SIZES = [16, 32, 64, 128, 256, 512, 1024, 2048, 4096, 8192]
-# (equations per thread, threads per CTA, variant: 1 registers, 2 staged)
+# (equations per thread, threads per CTA, variant: 1 registers, 2 staged,
+# 3 swizzled staged with two stages, 4 swizzled with one stage)
 CANDIDATES = [(4, 128, 1), (4, 256, 1), (4, 512, 1), (4, 1024, 1),
               (8, 128, 1), (8, 256, 1), (8, 512, 1), (8, 1024, 1),
               (4, 128, 2), (4, 256, 2), (4, 512, 2),
-              (8, 128, 2), (8, 256, 2), (8, 512, 2)]
+              (8, 128, 2), (8, 256, 2), (8, 512, 2),
+              (8, 64, 3), (8, 128, 3), (8, 256, 3),
+              (16, 64, 3), (16, 128, 3), (16, 256, 3),
+              (8, 128, 4), (16, 64, 4), (16, 128, 4)]
+VARIANT_TAG = {1: "", 2: "s", 3: "w", 4: "w1"}
 
 
 def _device_name():
@@ -85,11 +90,11 @@ def tune(sizes=SIZES, refine_steps=1, verbose=True):
         best = None
         trials = {}
         for L, nt, v in CANDIDATES:
-            if n < 2 * L or n // L > nt:
+            if n < 2 * L or n // L > nt or (v >= 3 and n < 32):
                 continue
             ms, _ = time_tile(n, L, nt, v, refine_steps,
                               dev_arrays=(a, b, c, d))
-            trials[f"{L}x{nt}{'s' if v == 2 else ''}"] = ms
+            trials[f"{L}x{nt}{VARIANT_TAG[v]}"] = ms
             if best is None or ms < best[3]:
                 best = (L, nt, v, ms)
         table[str(n)] = {"eq_per_thread": best[0], "threads_per_cta": best[1],

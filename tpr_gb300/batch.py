@@ -55,7 +55,10 @@ def _declare(L):
             fn.argtypes = args
 
 
-REGISTERS, STAGED = 1, 2
+# kernel variants (tprgb_batch_opts.variant): inputs loaded to registers;
+# staged by TMA bulk copies; staged by swizzled tensor-map copies with two
+# stages; the same with one stage
+REGISTERS, STAGED, SWIZZLED, SWIZZLED_ONE = 1, 2, 3, 4
 
 
 def opts(refine_steps: int = 1, residual: int = RESID_DF, x_f64: bool = True,

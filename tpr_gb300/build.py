@@ -34,6 +34,7 @@ SOURCES = {
     "ref_kernels.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true"],
     "batch_kernels.cu": [],
     "batch_tma.cu": [],
+    "batch_sw.cu": [],
     "batch_api.cu": [],
     "plan_kernels.cu": [],
     "gen_kernels.cu": [],

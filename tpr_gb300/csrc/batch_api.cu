@@ -44,10 +44,12 @@ TPRGB_API int tprgb_batch_opts_default(tprgb_batch_opts *o) {
 
 TPRGB_API int tprgb_tune_set(int n, int eq_per_thread, int threads_per_cta,
                              int variant) {
-    if (variant < 0 || variant > 2) return fail(TPRGB_EINVAL, "variant %d", variant);
-    TileConfig c{eq_per_thread, threads_per_cta, variant == 2 ? 1 : 0};
-    if (c.staged && c.nt != 128 && c.nt != 256 && c.nt != 512)
+    if (variant < 0 || variant > 4) return fail(TPRGB_EINVAL, "variant %d", variant);
+    TileConfig c{eq_per_thread, threads_per_cta, variant >= 2 ? variant - 1 : 0};
+    if (c.staged == 1 && c.nt != 128 && c.nt != 256 && c.nt != 512)
         return fail(TPRGB_EINVAL, "staged tiles use 128, 256 or 512 threads");
+    if (c.staged >= 2 && ((c.nt != 64 && c.nt != 128 && c.nt != 256) || n < 32))
+        return fail(TPRGB_EINVAL, "swizzled tiles use 64, 128 or 256 threads and n >= 32");
     int rc = batch_config_check(n, c);
     if (rc) return rc;
     int k = ilog2(n);
@@ -62,7 +64,7 @@ TPRGB_API int tprgb_tune_get(int n, int *eq_per_thread, int *threads_per_cta,
     TileConfig c = tuned_tile(n);
     if (eq_per_thread) *eq_per_thread = c.L;
     if (threads_per_cta) *threads_per_cta = c.nt;
-    if (variant) *variant = c.staged ? 2 : 1;
+    if (variant) *variant = c.staged + 1;
     return TPRGB_OK;
 }
 
@@ -92,21 +94,30 @@ TPRGB_API int tprgb_batch_solve(int nsys, int n, const float *d_a,
                           (const void *)d_x})
         if (((uintptr_t)p & 15) != 0)
             return fail(TPRGB_EINVAL, "device arrays must be 16-byte aligned");
-    if (o.variant < 0 || o.variant > 2)
+    if (o.variant < 0 || o.variant > 4)
         return fail(TPRGB_EINVAL, "unknown kernel variant %d", o.variant);
     TileConfig cfg = tuned_tile(n);
     if (o.eq_per_thread) cfg.L = o.eq_per_thread;
     if (o.threads_per_cta) cfg.nt = o.threads_per_cta;
-    if (o.variant) cfg.staged = o.variant == 2 ? 1 : 0;
+    if (o.variant) cfg.staged = o.variant - 1;
     BatchArgs A{d_a, d_b, d_c, d_d, d_x, nsys, n, o.refine_steps, o.residual,
                 o.x_f64};
-    const bool staged_ok = (cfg.nt == 128 || cfg.nt == 256 || cfg.nt == 512) &&
-                           !(o.residual == TPRGB_RESID_F64 && o.refine_steps > 0);
-    if (cfg.staged && staged_ok)
+    const bool f64_resid = o.residual == TPRGB_RESID_F64 && o.refine_steps > 0;
+    const bool staged_ok = (cfg.nt == 128 || cfg.nt == 256 || cfg.nt == 512) && !f64_resid;
+    const bool sw_ok = (cfg.nt == 64 || cfg.nt == 128 || cfg.nt == 256) && n >= 32 &&
+                       (cfg.L == 8 || cfg.L == 16) && !f64_resid;
+    if (cfg.staged >= 2 && sw_ok) return launch_batch_sw(A, cfg, (cudaStream_t)stream);
+    if (cfg.staged == 1 && staged_ok)
         return launch_batch_tma(A, cfg, (cudaStream_t)stream);
-    if (o.variant == 2)
+    if (o.variant >= 2)
         return fail(TPRGB_EUNSUPPORTED,
-                    "staged kernel needs 128/256/512 threads and the compensated residual");
+                    "variant %d does not serve this tile (threads %d, n %d) or residual",
+                    o.variant, cfg.nt, n);
+    // a tuned staged tile that cannot serve this call (FP64 residual): the
+    // register kernel with the same shape where that is valid
+    if (cfg.L == 16) cfg.L = 8;
+    if (cfg.nt < 128) cfg.nt = 128;
+    cfg.staged = 0;
     return launch_batch_uniform(A, cfg, (cudaStream_t)stream);
 }
 

@@ -99,8 +99,9 @@ static int launch_uniform_nt(const BatchArgs &A, int nt, cudaStream_t st) {
 }
 
 int batch_config_check(int n, const TileConfig &cfg) {
-    if (cfg.L != 4 && cfg.L != 8)
-        return fail(TPRGB_EINVAL, "equations per thread %d not in {4, 8}", cfg.L);
+    if (cfg.staged >= 2 ? (cfg.L != 8 && cfg.L != 16) : (cfg.L != 4 && cfg.L != 8))
+        return fail(TPRGB_EINVAL, "equations per thread %d not in %s", cfg.L,
+                    cfg.staged >= 2 ? "{8, 16}" : "{4, 8}");
     if (!is_pow2(n) || n < 2 * cfg.L)
         return fail(TPRGB_EINVAL, "n=%d must be a power of two >= %d", n, 2 * cfg.L);
     const int T = n / cfg.L;

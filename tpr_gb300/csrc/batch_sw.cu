@@ -1,0 +1,241 @@
+// Uniform batches staged by swizzled 2D tensor-map loads.
+//
+// Each array's tile is one box of a 2D tensor map (rows of 128 bytes, 32
+// floats) loaded with the 128-byte swizzle: unit u (16 bytes) of row r
+// lands at unit u ^ (r & 7), so the lanes of a warp reading their own
+// chunks' units spread over all 32 banks (a contiguous layout puts lanes
+// whose chunks are 32 or 64 bytes apart on the same banks).  Persistent
+// CTAs walk the batch with a one- or two-stage ring; 8 or 16 equations per
+// thread.  Every mbarrier wait is bounded; a timeout is recorded in this
+// unit's status word and the CTA stops after draining its copies.
+#include <cuda.h>  // CUtensorMap and its enums (the encoder is fetched at run time)
+
+#include <algorithm>
+
+#include "batch.cuh"
+#include "tile.cuh"
+#include "tma.cuh"
+
+namespace tprgb {
+
+__device__ unsigned g_sw_status[4];  // code, where, tile, unused
+
+namespace bt {
+
+constexpr unsigned kWaitLimit = 1u << 22;  // polls (~0.3 s with back-off)
+
+// ---- tensor-map (swizzled) staging ----------------------------------------
+struct TensorMaps {
+    CUtensorMap m[4];  // a, b, c, d as [rows][32 floats]
+};
+
+// Registers a thread may use so that the tile's CTAs fit the register file:
+// 128 for 16 equations per thread, 80 below.
+constexpr int sw_min_blocks(int L, int NT) {
+    return (65536 / (NT * (L >= 16 ? 128 : 80))) < 1 ? 1
+                                                      : 65536 / (NT * (L >= 16 ? 128 : 80));
+}
+
+template <int L, int NT, int T, int MODE>
+__global__ void __launch_bounds__(NT, sw_min_blocks(L, NT))
+batch_sw(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
+         int refine_steps, int x_f64, int S) {
+    constexpr int TILE = NT * L;     // equations per tile
+    constexpr int ROWS = TILE / 32;  // 128-byte rows per array and tile
+    constexpr int G = NT / T;
+    constexpr int n = T * L;
+    static_assert(ROWS % 8 == 0 && ROWS <= 256, "tile rows");
+    extern __shared__ unsigned char dyn_sw[];
+    // stage base on a 1024-byte boundary: the swizzle pattern spans 8 rows
+    const unsigned pad = (1024u - (tma::smem_addr(dyn_sw) & 1023u)) & 1023u;
+    float *stages = reinterpret_cast<float *>(dyn_sw + pad);  // [S][4][TILE]
+    __shared__ __align__(8) uint64_t full[2];
+    __shared__ tile::Smem<NT> sm;
+    __shared__ int s_ok;
+    const int tid = threadIdx.x;
+    const long long ntiles = ((long long)nsys + G - 1) / G;
+
+    if (tid == 0) {
+        tma::mbar_init(&full[0], 1);
+        tma::mbar_init(&full[1], 1);
+        tma::fence_barrier_init();
+    }
+    __syncthreads();
+
+    auto issue = [&](long long tl, int st) {  // thread 0 only
+        tma::fence_proxy_async();
+        // the whole box counts, rows past the end are zero-filled
+        tma::mbar_expect_tx(&full[st], 4u * TILE * 4u);
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            tma::tensor_g2s_2d(stages + (st * 4 + k) * TILE, &tm.m[k], 0,
+                               (int)(tl * ROWS), &full[st]);
+    };
+
+    const long long first = blockIdx.x, stride = gridDim.x;
+    if (tid == 0) {
+        if (first < ntiles) issue(first, 0);
+        if (S == 2 && first + stride < ntiles) issue(first + stride, 1);
+    }
+    unsigned off[L / 4];
+    tile::swizzled_offsets<L>(tid, off);
+    const int g = tid / T, t = tid & (T - 1);
+    int it = 0;
+    for (long long tl = first; tl < ntiles; tl += stride, it++) {
+        const int st = S == 2 ? (it & 1) : 0;
+        const unsigned phase = (unsigned)(S == 2 ? (it >> 1) : it) & 1u;
+        if (tid == 0) {
+            s_ok = tma::mbar_wait(&full[st], phase, kWaitLimit) ? 1 : 0;
+            if (!s_ok) {
+                atomicCAS(&g_sw_status[0], 0u, (unsigned)TPRGB_ETIMEOUT);
+                g_sw_status[1] = 2;
+                g_sw_status[2] = (unsigned)tl;
+            }
+        }
+        __syncthreads();
+        if (!s_ok) {
+            if (S == 2 && tid == 0 && tl + stride < ntiles)
+                tma::mbar_wait(&full[st ^ 1], (unsigned)((it + 1) >> 1) & 1u,
+                               kWaitLimit);
+            return;
+        }
+        const long long sys = tl * G + g;
+        const bool active = sys < nsys;
+        tile::Part pc;
+        pc.on = 0;
+        pc.P = 1;
+        pc.p = 0;
+        pc.round = 0;
+        const float *s0 = stages + st * 4 * TILE;
+        tile::run_tile_smem<L, NT, T, MODE, true>(
+            s0, s0 + TILE, s0 + 2 * TILE, s0 + 3 * TILE, off, gx,
+            active ? sys * n + (long long)t * L : 0, active, t, t == 0,
+            t == T - 1, refine_steps, x_f64, sm, pc);
+        __syncthreads();  // every thread is done reading this stage
+        if (tid == 0 && tl + (long long)S * stride < ntiles)
+            issue(tl + (long long)S * stride, st);
+    }
+}
+
+}  // namespace bt
+
+// ---- swizzled variant: host side -------------------------------------------
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t,
+                                 void *, const cuuint64_t *, const cuuint64_t *,
+                                 const cuuint32_t *, const cuuint32_t *,
+                                 CUtensorMapInterleave, CUtensorMapSwizzle,
+                                 CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static int tensor_encoder(EncodeTiled *out) {
+    static EncodeTiled fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p,
+                                                         12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p)
+            return fail(TPRGB_EUNSUPPORTED, "cuTensorMapEncodeTiled is not available");
+        fn = reinterpret_cast<EncodeTiled>(p);
+    }
+    *out = fn;
+    return TPRGB_OK;
+}
+
+template <int L, int NT, int T, int MODE>
+static int launch_sw_t(const BatchArgs &A, int S, cudaStream_t st) {
+    constexpr int G = NT / T;
+    constexpr int ROWS = NT * L / 32;
+    const size_t smem = (size_t)S * 4 * NT * L * sizeof(float) + 1024;
+    auto k = bt::batch_sw<L, NT, T, MODE>;
+    static int grid_cap[3] = {0, 0, 0};
+    if (!grid_cap[S]) {
+        const size_t smax = 2ull * 4 * NT * L * sizeof(float) + 1024;
+        TPRGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smax));
+        int dev = 0, sms = 0, per = 0;
+        TPRGB_CUDA(cudaGetDevice(&dev));
+        TPRGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        TPRGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, NT, smem));
+        grid_cap[S] = std::max(1, sms * std::max(per, 1));
+    }
+    EncodeTiled enc = nullptr;
+    int rc = tensor_encoder(&enc);
+    if (rc) return rc;
+    bt::TensorMaps tm;
+    const cuuint64_t total = (cuuint64_t)A.nsys * (cuuint64_t)A.n;
+    const cuuint64_t dims[2] = {32, total / 32};
+    const cuuint64_t strides[1] = {128};
+    const cuuint32_t box[2] = {32, (cuuint32_t)ROWS};
+    const cuuint32_t es[2] = {1, 1};
+    const float *src[4] = {A.a, A.b, A.c, A.d};
+    for (int i = 0; i < 4; i++) {
+        CUresult r = enc(&tm.m[i], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                         const_cast<float *>(src[i]), dims, strides, box, es,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS)
+            return fail(TPRGB_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    }
+    const long long ntiles = (A.nsys + G - 1) / G;
+    const int grid = (int)std::min<long long>(ntiles, grid_cap[S]);
+    k<<<grid, NT, smem, st>>>(tm, A.x, A.nsys, A.refine_steps, A.x_f64, S);
+    TPRGB_CUDA(cudaGetLastError());
+    return TPRGB_OK;
+}
+
+template <int L, int NT, int T>
+static int launch_sw_mode(const BatchArgs &A, int S, cudaStream_t st) {
+    if (A.refine_steps <= 0) return launch_sw_t<L, NT, T, 0>(A, S, st);
+    return launch_sw_t<L, NT, T, 1>(A, S, st);
+}
+
+template <int L, int NT>
+static int launch_sw_T(const BatchArgs &A, int S, cudaStream_t st) {
+    switch (A.n / L) {
+        case 2: return launch_sw_mode<L, NT, 2>(A, S, st);
+        case 4: return launch_sw_mode<L, NT, 4>(A, S, st);
+        case 8: return launch_sw_mode<L, NT, 8>(A, S, st);
+        case 16: return launch_sw_mode<L, NT, 16>(A, S, st);
+        case 32: return launch_sw_mode<L, NT, 32>(A, S, st);
+        case 64: return launch_sw_mode<L, NT, 64>(A, S, st);
+        case 128: return launch_sw_mode<L, NT, (NT >= 128 ? 128 : NT)>(A, S, st);
+        case 256: return launch_sw_mode<L, NT, (NT >= 256 ? 256 : NT)>(A, S, st);
+        default: return fail(TPRGB_EINVAL, "unsupported threads per system");
+    }
+}
+
+// Swizzled staged batch: L in {8, 16}, nt in {64, 128, 256}, n >= 32,
+// compensated residual; S = 2 (two-stage ring) or 1 (one stage, more
+// resident CTAs).
+int launch_batch_sw(const BatchArgs &A, const TileConfig &cfg, cudaStream_t st) {
+    int rc = batch_config_check(A.n, cfg);
+    if (rc) return rc;
+    if (A.residual == TPRGB_RESID_F64 && A.refine_steps > 0)
+        return fail(TPRGB_EUNSUPPORTED, "staged kernel has no FP64 residual mode");
+    if (cfg.nt != 64 && cfg.nt != 128 && cfg.nt != 256)
+        return fail(TPRGB_EINVAL, "swizzled tiles use 64, 128 or 256 threads");
+    if (A.n < 32)
+        return fail(TPRGB_EUNSUPPORTED, "swizzled tiles need n >= 32");
+    if (A.nsys == 0) return TPRGB_OK;
+    const int S = cfg.staged == 2 ? 2 : 1;
+    if (cfg.L == 16) {
+        if (cfg.nt == 64) return launch_sw_T<16, 64>(A, S, st);
+        return cfg.nt == 128 ? launch_sw_T<16, 128>(A, S, st)
+                             : launch_sw_T<16, 256>(A, S, st);
+    }
+    if (cfg.L != 8) return fail(TPRGB_EINVAL, "swizzled tiles use 8 or 16 equations per thread");
+    if (cfg.nt == 64) return launch_sw_T<8, 64>(A, S, st);
+    return cfg.nt == 128 ? launch_sw_T<8, 128>(A, S, st) : launch_sw_T<8, 256>(A, S, st);
+}
+
+int sw_status(unsigned (&v)[4], bool reset) {
+    TPRGB_CUDA(cudaMemcpyFromSymbol(v, g_sw_status, sizeof(v)));
+    if (reset) {
+        unsigned z[4] = {0, 0, 0, 0};
+        TPRGB_CUDA(cudaMemcpyToSymbol(g_sw_status, z, sizeof(z)));
+    }
+    return TPRGB_OK;
+}
+
+}  // namespace tprgb

@@ -88,14 +88,15 @@ batch_tma(const float *__restrict__ ga, const float *__restrict__ gb,
         const long long sys = tl * G + g;
         const bool active = sys < nsys;
         const float *base_s = stages + st * 4 * TILE + g * n + t * L;
+        const unsigned no_off[L / 4] = {};
         tile::Part pc;
         pc.on = 0;
         pc.P = 1;
         pc.p = 0;
         pc.round = 0;
         tile::run_tile_smem<L, NT, T, MODE>(
-            base_s, base_s + TILE, base_s + 2 * TILE, base_s + 3 * TILE, gx,
-            active ? sys * n + (long long)t * L : 0, active, t, t == 0,
+            base_s, base_s + TILE, base_s + 2 * TILE, base_s + 3 * TILE, no_off,
+            gx, active ? sys * n + (long long)t * L : 0, active, t, t == 0,
             t == T - 1, refine_steps, x_f64, sm, pc);
         __syncthreads();  // every thread is done reading this stage
         if (tid == 0 && tl + 2 * stride < ntiles) issue(tl + 2 * stride, st);
@@ -171,8 +172,12 @@ int launch_batch_tma(const BatchArgs &A, const TileConfig &cfg, cudaStream_t st)
 
 extern "C" TPRGB_API int tprgb_batch_status(unsigned *code, int reset) {
     using namespace tprgb;
-    unsigned v[4];
+    unsigned v[4], w[4];
     TPRGB_CUDA(cudaMemcpyFromSymbol(v, g_batch_status, sizeof(v)));
+    int rc = sw_status(w, reset != 0);
+    if (rc) return rc;
+    if (v[0] == 0 && w[0] != 0)
+        for (int i = 0; i < 4; i++) v[i] = w[i];
     if (code) *code = v[0];
     if (reset) {
         unsigned z[4] = {0, 0, 0, 0};

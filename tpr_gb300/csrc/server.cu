@@ -104,6 +104,8 @@ struct Request {
     const float *ha = nullptr, *hb = nullptr, *hc = nullptr, *hd = nullptr;
     double *hx = nullptr;
     Clock::time_point t_submit, t_done;
+    double queue_us = 0.0;  // submission -> the finishing step was enqueued
+    float step_us = 0.f;    // device time of the finishing step
     int state = 0;  // 0 pending, 1 admitted, 2 in step, 3 done, 4 failed
     int status = TPRGB_OK;
     unsigned nonfinite = 0;
@@ -124,7 +126,8 @@ struct Step {
     std::vector<int> order;  // sorted system -> flattened index
     std::vector<int> owner;  // flattened index -> entry of parts
     int nsys = 0;
-    cudaEvent_t done = nullptr;
+    cudaEvent_t start = nullptr, done = nullptr;
+    Clock::time_point t_launch;
     int buf = 0;
 };
 
@@ -160,6 +163,7 @@ struct Server {
     } gen[2];
     int gen_next = 0;
     cudaEvent_t step_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t start_ev[4] = {nullptr, nullptr, nullptr, nullptr};
     int mode = 1, grid = 0;
 
     std::mutex mu;
@@ -337,6 +341,9 @@ static int launch_step(Server *s) {
     std::fill(b.h_ctl, b.h_ctl + ctl_words, 0u);
     b.h_ctl[1] = (unsigned)(16 + nlarge);
     cudaStream_t cs = s->comp;
+    st.start = s->start_ev[st.id & 3];
+    st.t_launch = Clock::now();
+    TPRGB_CUDA(cudaEventRecord(st.start, cs));
     TPRGB_CUDA(cudaEventRecord(s->prep_ev[st.buf], s->prep));
     TPRGB_CUDA(cudaStreamWaitEvent(cs, s->prep_ev[st.buf], 0));
     TPRGB_CUDA(cudaMemcpyAsync(b.items, b.h_items, sizeof(int4) * items.size(),
@@ -375,6 +382,8 @@ static void finish_step(Server *s, Step &st) {
     const unsigned code = b.h_ctl[4];
     const unsigned nlarge = b.h_ctl[1] - 16;
     auto now = Clock::now();
+    float step_ms = 0.f;
+    if (cudaEventElapsedTime(&step_ms, st.start, st.done) != cudaSuccess) step_ms = 0.f;
     for (int k = 0; k < st.nsys; k++)
         if (b.h_ctl[16 + nlarge + k]) st.parts[st.owner[st.order[k]]].req->nonfinite++;
     for (auto &pt : st.parts) {
@@ -384,6 +393,9 @@ static void finish_step(Server *s, Step &st) {
         s->systems_done += pt.count;
         if (r.unfinished == 0 && r.next_sys == r.nsys) {
             r.t_done = now;
+            r.queue_us =
+                std::chrono::duration<double, std::micro>(st.t_launch - r.t_submit).count();
+            r.step_us = step_ms * 1e3f;
             r.state = 3;
             r.step = st.id;
             if (r.timed_out)
@@ -441,8 +453,8 @@ static void scheduler(Server *s) {
             }
             if (rc) s->cv_done.notify_all();
         }
-        // 3. next step: keep at most two in flight
-        if (!s->ready.empty() && s->inflight.size() < 2) {
+        // 3. next step: keep at most max_inflight (1 or 2) in flight
+        if (!s->ready.empty() && (int)s->inflight.size() < s->o.max_inflight) {
             int rc = launch_step(s);
             if (rc) {
                 s->fatal = rc;
@@ -490,6 +502,8 @@ static void server_free(Server *s) {
         if (g.ev) cudaEventDestroy(g.ev);
     }
     for (auto &e : s->step_ev)
+        if (e) cudaEventDestroy(e);
+    for (auto &e : s->start_ev)
         if (e) cudaEventDestroy(e);
     cudaFree(s->A);
     for (int i = 0; i < 2; i++)
@@ -553,6 +567,7 @@ TPRGB_API int tprgb_server_opts_default(tprgb_server_opts *o) {
     o->residual = TPRGB_RESID_DF;
     o->threads_per_cta = 256;
     o->max_step_eq = 0;
+    o->max_inflight = 2;
     return TPRGB_OK;
 }
 
@@ -568,6 +583,10 @@ TPRGB_API int tprgb_server_create(const tprgb_server_opts *opts,
     if (s->o.threads_per_cta != 256 && s->o.threads_per_cta != 512) {
         delete s;
         return fail(TPRGB_EINVAL, "threads_per_cta must be 256 or 512");
+    }
+    if (s->o.max_inflight != 1 && s->o.max_inflight != 2) {
+        delete s;
+        return fail(TPRGB_EINVAL, "max_inflight must be 1 or 2");
     }
     s->mode = s->o.refine_steps <= 0 ? 0 : (s->o.residual == TPRGB_RESID_F64 ? 2 : 1);
     s->cap_eq = (long long)(s->o.budget_bytes / 24) & ~3LL;
@@ -597,7 +616,9 @@ TPRGB_API int tprgb_server_create(const tprgb_server_opts *opts,
         return fail(TPRGB_ECUDA, "server streams");
     }
     for (auto &e : s->step_ev)
-        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) rc = TPRGB_ECUDA;
+        if (cudaEventCreateWithFlags(&e, cudaEventDefault) != cudaSuccess) rc = TPRGB_ECUDA;
+    for (auto &e : s->start_ev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDefault) != cudaSuccess) rc = TPRGB_ECUDA;
     for (auto &g : s->gen) {
         if (cudaEventCreateWithFlags(&g.ev, cudaEventDisableTiming) != cudaSuccess) rc = TPRGB_ECUDA;
         if (!rc) rc = gen_reserve(g, 1 << 16);
@@ -674,6 +695,8 @@ TPRGB_API int tprgb_server_wait(tprgb_server *srv, uint64_t ticket,
             std::chrono::duration<double, std::micro>(r->t_done - r->t_submit).count();
         info->x_offset = r->at;
         info->neq = r->neq;
+        info->queue_us = r->queue_us;
+        info->step_us = r->step_us;
     }
     return r->status;
 }
@@ -754,7 +777,7 @@ TPRGB_API int tprgb_server_get_stats(tprgb_server *srv, tprgb_server_stats *st) 
 extern "C" TPRGB_API int tprgb_server_run_load(
     tprgb_server *srv, int nreq, double rate_per_s, uint64_t seed, int min_sys,
     int max_sys, int kmin, int kmax, int kind, double *latencies_us,
-    double *elapsed_s, long long *systems_out) {
+    double *detail_us, double *elapsed_s, long long *systems_out) {
     using namespace tprgb;
     if (!srv || nreq <= 0 || min_sys < 1 || max_sys < min_sys || kmin < 4 ||
         kmax < kmin || kmax > 30)
@@ -805,12 +828,18 @@ extern "C" TPRGB_API int tprgb_server_run_load(
         if (sub_rc[i]) {
             if (!first_err) first_err = sub_rc[i];
             if (latencies_us) latencies_us[i] = -1.0;
+            if (detail_us) detail_us[3 * i] = detail_us[3 * i + 1] = detail_us[3 * i + 2] = -1.0;
             continue;
         }
         tprgb_request_info info;
         int rc = tprgb_server_wait(srv, tickets[i], -1, &info);
         if (rc && !first_err) first_err = rc;
         if (latencies_us) latencies_us[i] = info.latency_us;
+        if (detail_us) {
+            detail_us[3 * i] = info.queue_us;
+            detail_us[3 * i + 1] = info.step_us;
+            detail_us[3 * i + 2] = (double)info.neq;
+        }
         tprgb_server_release(srv, tickets[i]);
         last = Clock::now();
     }

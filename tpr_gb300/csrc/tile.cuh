@@ -392,6 +392,11 @@ __device__ __forceinline__ bool run_tile(
 
 
 // ---- tile runner with the raw system staged in shared memory ---------------
+// A thread's chunk of one array is L/4 16-byte units at the byte offsets
+// off[0..L/4) from the array's base: consecutive for a plain staged tile,
+// permuted by the 128-byte swizzle of a tensor-map load (unit u of 128-byte
+// row r sits at unit u ^ (r & 7)), which spreads the lanes of a warp over
+// all 32 banks.
 template <int L>
 __device__ __forceinline__ void lds_chunk(const float *p, float (&v)[L]) {
     const float4 *q = reinterpret_cast<const float4 *>(p);
@@ -405,21 +410,58 @@ __device__ __forceinline__ void lds_chunk(const float *p, float (&v)[L]) {
     }
 }
 
+// Swizzled form: unit i of the chunk at byte offset off[i] from `base`.
+template <int L>
+__device__ __forceinline__ void lds_chunk_sw(const float *base,
+                                             const unsigned (&off)[L / 4],
+                                             float (&v)[L]) {
+    const char *p = reinterpret_cast<const char *>(base);
+#pragma unroll
+    for (int i = 0; i < L / 4; i++) {
+        float4 t = *reinterpret_cast<const float4 *>(p + off[i]);
+        v[4 * i + 0] = t.x;
+        v[4 * i + 1] = t.y;
+        v[4 * i + 2] = t.z;
+        v[4 * i + 3] = t.w;
+    }
+}
+
+// Byte offsets of the 16-byte units of tile-thread `tid`'s chunk (L
+// equations per thread) in an array region written by a tensor-map load
+// with the 128-byte swizzle.
+template <int L>
+__device__ __forceinline__ void swizzled_offsets(int tid, unsigned (&off)[L / 4]) {
+    const unsigned b0 = (unsigned)tid * L * 4u;
+    const unsigned r7 = (b0 >> 7) & 7u;
+#pragma unroll
+    for (int j = 0; j < L / 4; j++) off[j] = b0 ^ ((((unsigned)j) ^ r7) << 4);
+}
+
 // Same computation as run_tile, but a, b, c, d are re-read from shared
-// memory (sa..sd: this thread's chunk) each time they are needed instead
-// of being held in registers through the refinement.
-template <int L, int NT, int T, int MODE>
+// memory each time they are needed instead of being held in registers
+// through the refinement.  SW = false: sa..sd point at this thread's
+// contiguous chunk; SW = true: sa..sd are the array regions' bases and off
+// holds the chunk's swizzled unit offsets.
+template <int L, int NT, int T, int MODE, bool SW = false>
 __device__ __forceinline__ bool run_tile_smem(
     const float *sa, const float *sb, const float *sc, const float *sd,
-    void *__restrict__ gx, long long base, bool active, int t, bool first_eq,
-    bool last_eq, int refine_steps, int x_f64, Smem<NT> &sm, Part &pc) {
+    const unsigned (&off)[L / 4], void *__restrict__ gx, long long base,
+    bool active, int t, bool first_eq, bool last_eq, int refine_steps,
+    int x_f64, Smem<NT> &sm, Part &pc) {
     auto load4 = [&](float (&a)[L], float (&b)[L], float (&c)[L],
                      float (&d)[L]) {
         if (active) {
-            lds_chunk<L>(sa, a);
-            lds_chunk<L>(sb, b);
-            lds_chunk<L>(sc, c);
-            lds_chunk<L>(sd, d);
+            if (SW) {
+                lds_chunk_sw<L>(sa, off, a);
+                lds_chunk_sw<L>(sb, off, b);
+                lds_chunk_sw<L>(sc, off, c);
+                lds_chunk_sw<L>(sd, off, d);
+            } else {
+                lds_chunk<L>(sa, a);
+                lds_chunk<L>(sb, b);
+                lds_chunk<L>(sc, c);
+                lds_chunk<L>(sd, d);
+            }
         } else {
 #pragma unroll
             for (int i = 0; i < L; i++) {

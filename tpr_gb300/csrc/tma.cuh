@@ -46,6 +46,18 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src,
         : "memory");
 }
 
+// One box of a 2D tensor map (x: innermost coordinate in elements, a
+// multiple of 16 bytes; y: row) global -> shared, completing the box's
+// bytes on `bar`.  tmap: address of a __grid_constant__ CUtensorMap.
+__device__ __forceinline__ void tensor_g2s_2d(void *dst, const void *tmap,
+                                              int x, int y, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::"
+        "complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_addr(dst)),
+        "l"(tmap), "r"(x), "r"(y), "r"(smem_addr(bar))
+        : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned phase) {
     uint32_t ok;
     asm volatile(

@@ -19,13 +19,15 @@ from .devgen import KIND
 class ServerOpts(C.Structure):
     _fields_ = [("budget_bytes", C.c_size_t), ("max_pending", C.c_int),
                 ("refine_steps", C.c_int), ("residual", C.c_int),
-                ("threads_per_cta", C.c_int), ("max_step_eq", C.c_longlong)]
+                ("threads_per_cta", C.c_int), ("max_step_eq", C.c_longlong),
+                ("max_inflight", C.c_int)]
 
 
 class RequestInfo(C.Structure):
     _fields_ = [("status", C.c_int), ("nonfinite_systems", C.c_int),
                 ("step", C.c_longlong), ("latency_us", C.c_double),
-                ("x_offset", C.c_longlong), ("neq", C.c_longlong)]
+                ("x_offset", C.c_longlong), ("neq", C.c_longlong),
+                ("queue_us", C.c_double), ("step_us", C.c_double)]
 
 
 class ServerStats(C.Structure):
@@ -51,7 +53,7 @@ def _declare(L):
         "tprgb_server_release": (i, [vp, u64]),
         "tprgb_server_get_stats": (i, [vp, C.POINTER(ServerStats)]),
         "tprgb_server_run_load": (i, [vp, i, C.c_double, u64, i, i, i, i, i,
-                                      vp, C.POINTER(C.c_double),
+                                      vp, vp, C.POINTER(C.c_double),
                                       C.POINTER(C.c_longlong)]),
     }
     for name, (res, args) in sig.items():
@@ -63,7 +65,8 @@ def _declare(L):
 class Server:
     def __init__(self, budget_bytes: int = 8 << 30, refine_steps: int = 1,
                  residual: int = 0, threads_per_cta: int = 256,
-                 max_pending: int = 1 << 20, max_step_eq: int = 0):
+                 max_pending: int = 1 << 20, max_step_eq: int = 0,
+                 max_inflight: int = 2):
         L = load()
         _declare(L)
         o = ServerOpts()
@@ -74,6 +77,7 @@ class Server:
         o.threads_per_cta = threads_per_cta
         o.max_pending = max_pending
         o.max_step_eq = max_step_eq
+        o.max_inflight = max_inflight
         self._h = C.c_void_p()
         self._keep = {}
         check(L.tprgb_server_create(C.byref(o), C.byref(self._h)))
@@ -132,13 +136,18 @@ class Server:
                  min_sys: int = 1, max_sys: int = 512, kmin: int = 8,
                  kmax: int = 14, kind: str = "uneven"):
         """Poisson load driven from a native thread; returns (latencies_us,
-        elapsed_s, systems, rc)."""
+        elapsed_s, systems, rc).  Per request queue time, device time of
+        its finishing step and equations are left in ``last_detail``
+        (nreq x 3, microseconds / count)."""
         lat = np.zeros(nreq, np.float64)
+        detail = np.zeros((nreq, 3), np.float64)
         el = C.c_double()
         nsys = C.c_longlong()
         rc = load().tprgb_server_run_load(
             self._h, nreq, float(rate_per_s), seed, min_sys, max_sys, kmin,
-            kmax, KIND[kind], lat.ctypes.data, C.byref(el), C.byref(nsys))
+            kmax, KIND[kind], lat.ctypes.data, detail.ctypes.data,
+            C.byref(el), C.byref(nsys))
+        self.last_detail = detail
         return lat, el.value, nsys.value, rc
 
     def close(self):
