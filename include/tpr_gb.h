@@ -184,7 +184,12 @@ typedef struct tprgb_batch_opts {
                                threads); 3: staged by swizzled 2D tensor-map
                                copies, two stages (8 or 16 equations per
                                thread, 64/128/256 threads, n >= 32);
-                            4: as 3 with one stage                         */
+                            4: as 3 with one stage;
+                            5: one system per thread-block cluster of
+                               P = n / (16 * threads) CTAs, P in {2, 4, 8,
+                               16}, rows exchanged in distributed shared
+                               memory (16 equations per thread, 64/128/256
+                               threads)                                    */
 } tprgb_batch_opts;
 
 /* Defaults: 1 refinement step, compensated residual, FP64 x, tuned tile. */
@@ -192,7 +197,8 @@ TPRGB_API int tprgb_batch_opts_default(tprgb_batch_opts *opts);
 
 /* Solve nsys systems of size n laid out back to back (system k at element
  * k*n of every array).  n a power of two with 2*L <= n <= L * threads per
- * CTA (8192 with the default tiles); larger systems go through a plan.
+ * CTA (8192 with the default tiles), or up to 16 * 16 * threads (65536)
+ * with the cluster variant, the default above 8192.
  * Asynchronous on `stream`; allocates nothing; can be captured in a CUDA
  * graph. */
 TPRGB_API int tprgb_batch_solve(int nsys, int n, const float *d_a,

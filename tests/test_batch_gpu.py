@@ -162,3 +162,48 @@ def test_swizzled_rejects_bad_tiles(cuda):
     with pytest.raises(T.TprError):   # FP64 residual
         B.solve_host(bt, eq_per_thread=8, threads_per_cta=64,
                      variant=B.SWIZZLED, residual=B.RESID_F64)
+
+
+@pytest.mark.parametrize("n,nt,nsys", [(2048, 64, 5), (4096, 128, 3),
+                                       (8192, 64, 9), (16384, 256, 4),
+                                       (16384, 64, 100), (32768, 256, 3),
+                                       (65536, 256, 40)])
+def test_cluster_kernel(cuda, port, n, nt, nsys):
+    """One system per thread-block cluster (P = n / (16 nt) CTAs, boundary
+    rows exchanged in distributed shared memory): refined solutions meet
+    1e-9 and plain FP32 1e-5 against FP64 Thomas; batches with more systems
+    than resident clusters walk the grid-stride loop."""
+    bt = G.uniform_batch(nsys, n, 91 + n + nt, "uneven")
+    xs = B.solve_host(bt, refine_steps=1, eq_per_thread=16, threads_per_cta=nt,
+                      variant=B.CLUSTER)
+    worst, _ = _err(port, bt, xs)
+    assert worst <= 1e-9, worst
+    x2 = B.solve_host(bt, refine_steps=2, eq_per_thread=16, threads_per_cta=nt,
+                      variant=B.CLUSTER)
+    worst2, _ = _err(port, bt, x2)
+    assert worst2 <= 1e-9, worst2
+    xp = B.solve_host(bt, refine_steps=0, x_f64=False, eq_per_thread=16,
+                      threads_per_cta=nt, variant=B.CLUSTER)
+    worst, _ = _err(port, bt, xp)
+    assert worst <= 1e-5, worst
+    import ctypes
+    code = ctypes.c_uint()
+    assert B.load().tprgb_batch_status(ctypes.byref(code), 1) == 0
+    assert code.value == 0
+
+
+def test_cluster_default_and_rejects(cuda, port):
+    """Above 8192 equations the default tile is the cluster variant; sizes
+    that need more than 16 or fewer than 2 CTAs are refused."""
+    bt = G.uniform_batch(2, 32768, 5, "dominant")
+    x = B.solve_host(bt, refine_steps=1)
+    worst, _ = _err(port, bt, x)
+    assert worst <= 1e-9, worst
+    with pytest.raises(T.TprError):   # 32 CTAs of 2048
+        B.solve_host(G.uniform_batch(1, 65536, 5, "dominant"),
+                     eq_per_thread=16, threads_per_cta=128, variant=B.CLUSTER)
+    with pytest.raises(T.TprError):   # one CTA
+        B.solve_host(G.uniform_batch(2, 1024, 5, "dominant"),
+                     eq_per_thread=16, threads_per_cta=64, variant=B.CLUSTER)
+    with pytest.raises(T.TprError):   # FP64 residual
+        B.solve_host(bt, refine_steps=1, residual=B.RESID_F64)

@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 from tests.conftest import GOLDEN
+import tpr_gb300 as T
 from tpr_gb300 import autotune, devgen
 from tpr_gb300 import generate as G
 from tpr_gb300 import nstab, pm
@@ -35,6 +36,15 @@ def test_tune_set_rejects_bad_tiles(lib):
     assert lib.tprgb_tune_set(1024, 8, 64, 1) == T.EUNSUPPORTED  # T > nt
     assert lib.tprgb_tune_set(1024, 8, 1024, 2) == T.EINVAL     # staged nt
     assert lib.tprgb_tune_set(1000, 8, 256, 1) == T.EINVAL      # n
+    assert lib.tprgb_tune_set(16, 8, 64, 3) == T.EINVAL        # swizzled n < 32
+    assert lib.tprgb_tune_set(1024, 16, 512, 4) == T.EINVAL    # swizzled nt
+    assert lib.tprgb_tune_set(1024, 16, 128, 1) == T.EINVAL    # L=16 registers
+    assert lib.tprgb_tune_set(65536, 16, 128, 5) == T.EINVAL   # 32 CTAs
+    assert lib.tprgb_tune_set(1024, 16, 64, 5) == T.EINVAL     # one CTA
+    assert lib.tprgb_tune_set(32768, 8, 256, 5) == T.EINVAL    # cluster L
+    assert lib.tprgb_tune_set(32768, 16, 256, 5) == T.OK
+    assert lib.tprgb_tune_set(1024, 16, 64, 4) == T.OK
+    lib.tprgb_tune_clear()
 
 
 def test_committed_table_is_valid():
@@ -45,8 +55,15 @@ def test_committed_table_is_valid():
     for n, ent in doc["tiles"].items():
         n = int(n)
         assert n & (n - 1) == 0
-        assert ent["eq_per_thread"] in (4, 8)
-        assert n // ent["eq_per_thread"] <= ent["threads_per_cta"]
+        assert ent["eq_per_thread"] in (4, 8, 16)
+        assert autotune.fits(n, ent["eq_per_thread"], ent["threads_per_cta"],
+                             ent.get("variant", 1))
+        # the library accepts the entry (checked without a GPU)
+        lib = T.load()
+        assert lib.tprgb_tune_set(n, ent["eq_per_thread"],
+                                  ent["threads_per_cta"],
+                                  ent.get("variant", 1)) == T.OK
+    T.load().tprgb_tune_clear()
 
 
 def test_generators_deterministic_and_dominant():

@@ -9,31 +9,30 @@ import numpy as np
 import pytest
 
 
-def _two_sum(a, b):
-    s = np.float32(a + b)
-    bb = np.float32(s - a)
-    e = np.float32(np.float32(a - np.float32(s - bb)) + np.float32(b - bb))
-    return s, e
+def f32_to_f64_normal(f):
+    """Bits of the double equal to a normal float, built as on the device
+    (hier::f32_to_f64_normal)."""
+    u = int(np.array(f, np.float32).view(np.uint32))
+    hi = (((u & 0x7FFFFFFF) >> 3) + 0x38000000) | (u & 0x80000000)
+    lo = (u << 29) & 0xFFFFFFFF
+    return float(np.array((hi << 32) | lo, np.uint64).view(np.float64))
+
+
+def fast_ok(h, l):
+    m = int(np.array(h, np.float32).view(np.uint32)) & 0x7FFFFFFF
+    el = int(np.array(l, np.float32).view(np.uint32)) & 0x7F800000
+    return (m - 0x1E000000) % (1 << 32) < 0x7F800000 - 0x1E000000 and \
+        el != 0x7F800000
 
 
 def emulate(hi, lo):
-    s, e = _two_sum(np.float32(hi), np.float32(lo))
-    u = int(np.array(s, np.float32).view(np.uint32))
-    ex = (u >> 23) & 0xFF
-    if ex < 53 or ex == 255:
-        return float(s) + float(e)
-    sign, mant = u & 0x80000000, u & 0x7FFFFF
-    ue = int(np.array(e, np.float32).view(np.uint32))
-    down = e != 0 and ((ue ^ u) & 0x80000000) != 0
-    sc = 306 - ex + (1 if (mant == 0 and down) else 0)
-    scale = np.array(sc << 23, np.uint32).view(np.float32)
-    prod = np.float32(np.float32(abs(e)) * scale)   # exact: a power of two
-    kk = int(np.rint(prod))                          # nearest, ties to even
-    k = -kk if down else kk
-    bits = ((sign | ((ex + 896) << 20) | (mant >> 3)) << 32) | \
-        ((mant & 7) << 29)
-    bits = (bits + k) & ((1 << 64) - 1)
-    return float(np.array(bits, np.uint64).view(np.float64))
+    """hier::pair_to_double step for step: a DADD (numpy float64 addition,
+    round to nearest even) of the two bit-built doubles, or of the exact
+    conversions on the slow route."""
+    h, l = np.float32(hi), np.float32(lo)
+    if fast_ok(h, l):
+        return f32_to_f64_normal(h) + f32_to_f64_normal(l)
+    return float(h) + float(l)
 
 
 def cases(seed=0, n=20000):
@@ -54,6 +53,12 @@ def cases(seed=0, n=20000):
         for m in (1.0, 1.5, -1.0):
             for t in (1e-45, -1e-45, 3e-39, -5.9e-39, 1.1e-38):
                 extra.append((np.float32(m * 2.0 ** e), np.float32(t)))
+    # the screen's edge: |hi| around 2^-67 with zero / subnormal lo
+    for e in (-68, -67, -66):
+        for t in (0.0, -0.0, 1e-45, -3e-39, 1.17e-38):
+            extra.append((np.float32(1.25 * 2.0 ** e), np.float32(t)))
+    # non-finite operands (slow route)
+    extra += [(np.inf, 1.0), (-np.inf, 0.0), (1.0, np.inf), (2.0, -np.inf)]
     # largest magnitudes
     for m in (3.4e38, -3.4e38, 2.0 ** 127, 1.7e38):
         for r in (2.0 ** -25, -2.0 ** -26, 0.3 * 2.0 ** -24):
@@ -72,6 +77,14 @@ def test_emulated_assembly_is_exact():
     hi, lo = cases()
     for h, l in zip(hi, lo):
         assert emulate(h, l) == float(h) + float(l), (h, l)
+
+
+def test_bit_built_double_is_exact_for_normal_floats():
+    rng = np.random.default_rng(3)
+    bits = rng.integers(0x00800000, 0x7F800000, 5000, dtype=np.int64)
+    bits = np.concatenate([bits, bits | 0x80000000]).astype(np.uint32)
+    for f in bits.view(np.float32):
+        assert f32_to_f64_normal(f) == float(f), f
 
 
 @pytest.mark.gpu

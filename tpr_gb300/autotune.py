@@ -26,7 +26,8 @@ from . import check, load
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 TABLE = os.path.join(PKG, "tuned_tiles.json")
-SIZES = [16, 32, 64, 128, 256, 512, 1024, 2048, 4096, 8192]
+SIZES = [16, 32, 64, 128, 256, 512, 1024, 2048, 4096, 8192, 16384, 32768,
+         65536]
 # (equations per thread, threads per CTA, variant: 1 registers, 2 staged,
 # 3 swizzled staged with two stages, 4 swizzled with one stage)
 CANDIDATES = [(4, 128, 1), (4, 256, 1), (4, 512, 1), (4, 1024, 1),
@@ -35,8 +36,16 @@ CANDIDATES = [(4, 128, 1), (4, 256, 1), (4, 512, 1), (4, 1024, 1),
               (8, 128, 2), (8, 256, 2), (8, 512, 2),
               (8, 64, 3), (8, 128, 3), (8, 256, 3),
               (16, 64, 3), (16, 128, 3), (16, 256, 3),
-              (8, 128, 4), (16, 64, 4), (16, 128, 4)]
-VARIANT_TAG = {1: "", 2: "s", 3: "w", 4: "w1"}
+              (8, 128, 4), (16, 64, 4), (16, 128, 4),
+              (16, 64, 5), (16, 128, 5), (16, 256, 5)]
+VARIANT_TAG = {1: "", 2: "s", 3: "w", 4: "w1", 5: "c"}
+
+
+def fits(n, L, nt, v):
+    """Whether tile (L, nt, variant v) serves systems of size n."""
+    if v == 5:
+        return n % (16 * nt) == 0 and 2 <= n // (16 * nt) <= 16
+    return not (n < 2 * L or n // L > nt or (v >= 3 and n < 32))
 
 
 def _device_name():
@@ -90,7 +99,7 @@ def tune(sizes=SIZES, refine_steps=1, verbose=True):
         best = None
         trials = {}
         for L, nt, v in CANDIDATES:
-            if n < 2 * L or n // L > nt or (v >= 3 and n < 32):
+            if not fits(n, L, nt, v):
                 continue
             ms, _ = time_tile(n, L, nt, v, refine_steps,
                               dev_arrays=(a, b, c, d))

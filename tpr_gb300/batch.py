@@ -57,8 +57,8 @@ def _declare(L):
 
 # kernel variants (tprgb_batch_opts.variant): inputs loaded to registers;
 # staged by TMA bulk copies; staged by swizzled tensor-map copies with two
-# stages; the same with one stage
-REGISTERS, STAGED, SWIZZLED, SWIZZLED_ONE = 1, 2, 3, 4
+# stages; the same with one stage; one system per thread-block cluster
+REGISTERS, STAGED, SWIZZLED, SWIZZLED_ONE, CLUSTER = 1, 2, 3, 4, 5
 
 
 def opts(refine_steps: int = 1, residual: int = RESID_DF, x_f64: bool = True,

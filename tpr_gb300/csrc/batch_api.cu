@@ -12,7 +12,8 @@ TileConfig default_tile(int n) {
     if (n <= 1024) return TileConfig{8, 256};
     if (n <= 2048) return TileConfig{8, 256};
     if (n <= 4096) return TileConfig{8, 512};
-    return TileConfig{8, 1024};
+    if (n <= 8192) return TileConfig{8, 1024};
+    return TileConfig{16, 256, 4};  // one cluster of n / 4096 CTAs per system
 }
 
 // Tuned tiles per log2(n) (set by the autotuner through tprgb_tune_set).
@@ -44,7 +45,7 @@ TPRGB_API int tprgb_batch_opts_default(tprgb_batch_opts *o) {
 
 TPRGB_API int tprgb_tune_set(int n, int eq_per_thread, int threads_per_cta,
                              int variant) {
-    if (variant < 0 || variant > 4) return fail(TPRGB_EINVAL, "variant %d", variant);
+    if (variant < 0 || variant > 5) return fail(TPRGB_EINVAL, "variant %d", variant);
     TileConfig c{eq_per_thread, threads_per_cta, variant >= 2 ? variant - 1 : 0};
     if (c.staged == 1 && c.nt != 128 && c.nt != 256 && c.nt != 512)
         return fail(TPRGB_EINVAL, "staged tiles use 128, 256 or 512 threads");
@@ -94,7 +95,7 @@ TPRGB_API int tprgb_batch_solve(int nsys, int n, const float *d_a,
                           (const void *)d_x})
         if (((uintptr_t)p & 15) != 0)
             return fail(TPRGB_EINVAL, "device arrays must be 16-byte aligned");
-    if (o.variant < 0 || o.variant > 4)
+    if (o.variant < 0 || o.variant > 5)
         return fail(TPRGB_EINVAL, "unknown kernel variant %d", o.variant);
     TileConfig cfg = tuned_tile(n);
     if (o.eq_per_thread) cfg.L = o.eq_per_thread;
@@ -106,6 +107,12 @@ TPRGB_API int tprgb_batch_solve(int nsys, int n, const float *d_a,
     const bool staged_ok = (cfg.nt == 128 || cfg.nt == 256 || cfg.nt == 512) && !f64_resid;
     const bool sw_ok = (cfg.nt == 64 || cfg.nt == 128 || cfg.nt == 256) && n >= 32 &&
                        (cfg.L == 8 || cfg.L == 16) && !f64_resid;
+    if (cfg.staged == 4) {
+        if (f64_resid)
+            return fail(TPRGB_EUNSUPPORTED, "systems of %d equations need the cluster "
+                                            "kernel, which has no FP64 residual mode", n);
+        return launch_batch_cl(A, cfg, (cudaStream_t)stream);
+    }
     if (cfg.staged >= 2 && sw_ok) return launch_batch_sw(A, cfg, (cudaStream_t)stream);
     if (cfg.staged == 1 && staged_ok)
         return launch_batch_tma(A, cfg, (cudaStream_t)stream);

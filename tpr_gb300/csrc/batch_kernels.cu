@@ -99,6 +99,10 @@ static int launch_uniform_nt(const BatchArgs &A, int nt, cudaStream_t st) {
 }
 
 int batch_config_check(int n, const TileConfig &cfg) {
+    if (cfg.staged == 4) {
+        int P = 0;
+        return cluster_parts(n, cfg, &P);
+    }
     if (cfg.staged >= 2 ? (cfg.L != 8 && cfg.L != 16) : (cfg.L != 4 && cfg.L != 8))
         return fail(TPRGB_EINVAL, "equations per thread %d not in %s", cfg.L,
                     cfg.staged >= 2 ? "{8, 16}" : "{4, 8}");

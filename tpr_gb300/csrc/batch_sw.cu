@@ -13,6 +13,7 @@
 #include <algorithm>
 
 #include "batch.cuh"
+#include "cluster.cuh"
 #include "tile.cuh"
 #include "tma.cuh"
 
@@ -36,10 +37,17 @@ constexpr int sw_min_blocks(int L, int NT) {
                                                       : 65536 / (NT * (L >= 16 ? 128 : 80));
 }
 
+// Systems at offsets: sys_off (element offsets, multiples of 32, n >= 256)
+// gives system k's first equation; the tensor maps' box is then one system
+// (n / 32 rows) and each tile is G box loads per array, issued by the
+// lanes of warp 0.  sys_off == nullptr: system k at k * n, one box per tile.
+// sys_status (may be null): word k |= 1 when system k's solution is not
+// finite.  status: timeout record (code, site, detail), g_sw_status if null.
 template <int L, int NT, int T, int MODE>
 __global__ void __launch_bounds__(NT, sw_min_blocks(L, NT))
 batch_sw(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
-         int refine_steps, int x_f64, int S) {
+         int refine_steps, int x_f64, int S, const long long *__restrict__ sys_off,
+         unsigned *__restrict__ sys_status, unsigned *__restrict__ status) {
     constexpr int TILE = NT * L;     // equations per tile
     constexpr int ROWS = TILE / 32;  // 128-byte rows per array and tile
     constexpr int G = NT / T;
@@ -54,6 +62,7 @@ batch_sw(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
     __shared__ int s_ok;
     const int tid = threadIdx.x;
     const long long ntiles = ((long long)nsys + G - 1) / G;
+    unsigned *stw = status ? status : g_sw_status;
 
     if (tid == 0) {
         tma::mbar_init(&full[0], 1);
@@ -62,18 +71,35 @@ batch_sw(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
     }
     __syncthreads();
 
-    auto issue = [&](long long tl, int st) {  // thread 0 only
+    auto issue = [&](long long tl, int st) {  // the lanes of warp 0
+        const int lane = tid & 31;
         tma::fence_proxy_async();
-        // the whole box counts, rows past the end are zero-filled
-        tma::mbar_expect_tx(&full[st], 4u * TILE * 4u);
+        if (!sys_off) {
+            if (lane == 0) {
+                // the whole box counts, rows past the end are zero-filled
+                tma::mbar_expect_tx(&full[st], 4u * TILE * 4u);
 #pragma unroll
-        for (int k = 0; k < 4; k++)
-            tma::tensor_g2s_2d(stages + (st * 4 + k) * TILE, &tm.m[k], 0,
-                               (int)(tl * ROWS), &full[st]);
+                for (int k = 0; k < 4; k++)
+                    tma::tensor_g2s_2d(stages + (st * 4 + k) * TILE, &tm.m[k], 0,
+                                       (int)(tl * ROWS), &full[st]);
+            }
+            return;
+        }
+        const long long s0 = tl * G;
+        const int gs = (int)min((long long)G, (long long)nsys - s0);
+        if (lane == 0) tma::mbar_expect_tx(&full[st], 4u * (unsigned)gs * n * 4u);
+        __syncwarp();
+        for (int g = lane; g < gs; g += 32) {
+            const int row = (int)(sys_off[s0 + g] >> 5);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                tma::tensor_g2s_2d(stages + (st * 4 + k) * TILE + g * n, &tm.m[k], 0,
+                                   row, &full[st]);
+        }
     };
 
     const long long first = blockIdx.x, stride = gridDim.x;
-    if (tid == 0) {
+    if (tid < 32) {
         if (first < ntiles) issue(first, 0);
         if (S == 2 && first + stride < ntiles) issue(first + stride, 1);
     }
@@ -87,9 +113,9 @@ batch_sw(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
         if (tid == 0) {
             s_ok = tma::mbar_wait(&full[st], phase, kWaitLimit) ? 1 : 0;
             if (!s_ok) {
-                atomicCAS(&g_sw_status[0], 0u, (unsigned)TPRGB_ETIMEOUT);
-                g_sw_status[1] = 2;
-                g_sw_status[2] = (unsigned)tl;
+                atomicCAS(&stw[0], 0u, (unsigned)TPRGB_ETIMEOUT);
+                stw[1] = 2;
+                stw[2] = (unsigned)tl;
             }
         }
         __syncthreads();
@@ -107,14 +133,113 @@ batch_sw(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
         pc.p = 0;
         pc.round = 0;
         const float *s0 = stages + st * 4 * TILE;
-        tile::run_tile_smem<L, NT, T, MODE, true>(
+        const long long sbase = active ? (sys_off ? sys_off[sys] : sys * n) : 0;
+        const bool finite = tile::run_tile_smem<L, NT, T, MODE, true>(
             s0, s0 + TILE, s0 + 2 * TILE, s0 + 3 * TILE, off, gx,
-            active ? sys * n + (long long)t * L : 0, active, t, t == 0,
+            active ? sbase + (long long)t * L : 0, active, t, t == 0,
             t == T - 1, refine_steps, x_f64, sm, pc);
+        if (sys_status && active && !finite) atomicOr(&sys_status[sys], 1u);
         __syncthreads();  // every thread is done reading this stage
-        if (tid == 0 && tl + (long long)S * stride < ntiles)
+        if (tid < 32 && tl + (long long)S * stride < ntiles)
             issue(tl + (long long)S * stride, st);
     }
+}
+
+// ---- systems spanning a thread-block cluster --------------------------------
+// One cluster of P CTAs per system of n = P * NT * L equations; CTA rank p
+// stages rows [p * ROWS, (p + 1) * ROWS) of the system's 128-byte rows with
+// a swizzled tensor-map load and solves its part; the parts' boundary rows
+// meet in distributed shared memory at cluster barriers (level 3).  Clusters
+// walk the batch with a stride of the number of clusters; every CTA of a
+// cluster runs the same number of systems and solves, so their cluster
+// barriers pair up.  A load that times out is recorded in the status word,
+// its CTA stores nothing for that system, and the CTA keeps taking part in
+// the barriers.  sys_off / sys_status / status as for batch_sw (offsets
+// multiples of 32).
+template <int L, int NT, int MODE>
+__global__ void __launch_bounds__(NT, sw_min_blocks(L, NT))
+batch_cl(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
+         int refine_steps, int x_f64, const long long *__restrict__ sys_off,
+         unsigned *__restrict__ sys_status, unsigned *__restrict__ status) {
+    constexpr int TILE = NT * L;
+    constexpr int ROWS = TILE / 32;
+    static_assert(ROWS % 8 == 0 && ROWS <= 256, "tile rows");
+    extern __shared__ unsigned char dyn_sw[];
+    const unsigned pad = (1024u - (tma::smem_addr(dyn_sw) & 1023u)) & 1023u;
+    float *stage = reinterpret_cast<float *>(dyn_sw + pad);  // [4][TILE]
+    __shared__ __align__(8) uint64_t full;
+    __shared__ tile::Smem<NT> sm;
+    __shared__ int s_ok;
+    const int tid = threadIdx.x;
+    const unsigned P = cl::size(), p = cl::rank();
+    const long long nclusters = gridDim.x / P, c0 = blockIdx.x / P;
+    const long long rows_per_sys = (long long)P * ROWS;
+    unsigned *stw = status ? status : g_sw_status;
+    auto sys_base = [&](long long sys) {  // first equation of a system
+        return sys_off ? sys_off[sys] : sys * rows_per_sys * 32;
+    };
+
+    if (tid == 0) {
+        tma::mbar_init(&full, 1);
+        tma::fence_barrier_init();
+    }
+    __syncthreads();
+    auto issue = [&](long long sys) {  // thread 0 only
+        tma::fence_proxy_async();
+        tma::mbar_expect_tx(&full, 4u * TILE * 4u);
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            tma::tensor_g2s_2d(stage + k * TILE, &tm.m[k], 0,
+                               (int)((sys_base(sys) >> 5) + (long long)p * ROWS), &full);
+    };
+    if (tid == 0 && c0 < nsys) issue(c0);
+    unsigned off[L / 4];
+    tile::swizzled_offsets<L>(tid, off);
+    unsigned round = 0;
+    // After a load times out, the CTA issues no more loads and solves its
+    // remaining parts on placeholder rows (storing nothing), so that its
+    // cluster barriers still pair with the other CTAs'; before leaving it
+    // waits, bounded, for the late copy.
+    bool pending = false;
+    unsigned pend_phase = 0;
+    int it = 0;
+    for (long long sys = c0; sys < nsys; sys += nclusters, it++) {
+        bool ok = false;
+        if (!pending) {
+            if (tid == 0) {
+                s_ok = tma::mbar_wait(&full, (unsigned)it & 1u, kWaitLimit) ? 1 : 0;
+                if (!s_ok) {
+                    atomicCAS(&stw[0], 0u, (unsigned)TPRGB_ETIMEOUT);
+                    stw[1] = 3;
+                    stw[2] = (unsigned)sys;
+                }
+            }
+            __syncthreads();
+            ok = s_ok != 0;
+            if (!ok) {
+                pending = true;
+                pend_phase = (unsigned)it & 1u;
+            }
+        }
+        tile::Part pc;
+        pc.on = 2;
+        pc.P = (int)P;
+        pc.p = (int)p;
+        pc.round = round;
+        pc.nsolve = 0;
+        const long long base = sys_base(sys) + (long long)p * TILE + tid * L;
+        const bool finite = tile::run_tile_smem<L, NT, NT, MODE, true>(
+            stage, stage + TILE, stage + 2 * TILE, stage + 3 * TILE, off, gx,
+            ok ? base : 0, ok, tid, p == 0 && tid == 0,
+            p == P - 1 && tid == NT - 1, refine_steps, x_f64, sm, pc);
+        if (sys_status && ok && !finite) atomicOr(&sys_status[sys], 1u);
+        round = pc.round;
+        __syncthreads();  // every thread is done reading the stage
+        if (tid == 0 && !pending && sys + nclusters < nsys) issue(sys + nclusters);
+    }
+    // no CTA leaves while another may still read its shared memory
+    cl::sync();
+    if (pending && tid == 0) tma::mbar_wait(&full, pend_phase, kWaitLimit);
 }
 
 }  // namespace bt
@@ -162,10 +287,11 @@ static int launch_sw_t(const BatchArgs &A, int S, cudaStream_t st) {
     int rc = tensor_encoder(&enc);
     if (rc) return rc;
     bt::TensorMaps tm;
-    const cuuint64_t total = (cuuint64_t)A.nsys * (cuuint64_t)A.n;
+    const cuuint64_t total =
+        A.total_eq ? (cuuint64_t)A.total_eq : (cuuint64_t)A.nsys * (cuuint64_t)A.n;
     const cuuint64_t dims[2] = {32, total / 32};
     const cuuint64_t strides[1] = {128};
-    const cuuint32_t box[2] = {32, (cuuint32_t)ROWS};
+    const cuuint32_t box[2] = {32, (cuuint32_t)(A.sys_off ? A.n / 32 : ROWS)};
     const cuuint32_t es[2] = {1, 1};
     const float *src[4] = {A.a, A.b, A.c, A.d};
     for (int i = 0; i < 4; i++) {
@@ -179,7 +305,8 @@ static int launch_sw_t(const BatchArgs &A, int S, cudaStream_t st) {
     }
     const long long ntiles = (A.nsys + G - 1) / G;
     const int grid = (int)std::min<long long>(ntiles, grid_cap[S]);
-    k<<<grid, NT, smem, st>>>(tm, A.x, A.nsys, A.refine_steps, A.x_f64, S);
+    k<<<grid, NT, smem, st>>>(tm, A.x, A.nsys, A.refine_steps, A.x_f64, S, A.sys_off,
+                              A.sys_status, A.status);
     TPRGB_CUDA(cudaGetLastError());
     return TPRGB_OK;
 }
@@ -227,6 +354,97 @@ int launch_batch_sw(const BatchArgs &A, const TileConfig &cfg, cudaStream_t st) 
     if (cfg.L != 8) return fail(TPRGB_EINVAL, "swizzled tiles use 8 or 16 equations per thread");
     if (cfg.nt == 64) return launch_sw_T<8, 64>(A, S, st);
     return cfg.nt == 128 ? launch_sw_T<8, 128>(A, S, st) : launch_sw_T<8, 256>(A, S, st);
+}
+
+// ---- cluster variant: host side ---------------------------------------------
+template <int L, int NT, int MODE>
+static int launch_cl_t(const BatchArgs &A, int P, cudaStream_t st) {
+    constexpr int TILE = NT * L;
+    constexpr int ROWS = TILE / 32;
+    const size_t smem = 4ull * TILE * sizeof(float) + 1024;
+    auto k = bt::batch_cl<L, NT, MODE>;
+    static int max_clusters[17] = {0};
+    static bool attrs = false;
+    if (!attrs) {
+        TPRGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+        TPRGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+        attrs = true;
+    }
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)P;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)P, 1, 1);
+    cfg.blockDim = dim3(NT, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (!max_clusters[P]) {
+        int num = 0;
+        TPRGB_CUDA(cudaOccupancyMaxActiveClusters(&num, k, &cfg));
+        if (num < 1)
+            return fail(TPRGB_EUNSUPPORTED, "a cluster of %d CTAs of %d threads does not fit",
+                        P, NT);
+        max_clusters[P] = num;
+    }
+    EncodeTiled enc = nullptr;
+    int rc = tensor_encoder(&enc);
+    if (rc) return rc;
+    bt::TensorMaps tm;
+    const cuuint64_t total =
+        A.total_eq ? (cuuint64_t)A.total_eq : (cuuint64_t)A.nsys * (cuuint64_t)A.n;
+    const cuuint64_t dims[2] = {32, total / 32};
+    const cuuint64_t strides[1] = {128};
+    const cuuint32_t box[2] = {32, (cuuint32_t)ROWS};
+    const cuuint32_t es[2] = {1, 1};
+    const float *src[4] = {A.a, A.b, A.c, A.d};
+    for (int i = 0; i < 4; i++) {
+        CUresult r = enc(&tm.m[i], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                         const_cast<float *>(src[i]), dims, strides, box, es,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS)
+            return fail(TPRGB_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    }
+    const int ncl = (int)std::min<long long>(A.nsys, max_clusters[P]);
+    cfg.gridDim = dim3((unsigned)(ncl * P), 1, 1);
+    TPRGB_CUDA(cudaLaunchKernelEx(&cfg, k, tm, A.x, A.nsys, A.refine_steps, A.x_f64,
+                                  A.sys_off, A.sys_status, A.status));
+    return TPRGB_OK;
+}
+
+template <int NT>
+static int launch_cl_mode(const BatchArgs &A, int P, cudaStream_t st) {
+    if (A.refine_steps <= 0) return launch_cl_t<16, NT, 0>(A, P, st);
+    return launch_cl_t<16, NT, 1>(A, P, st);
+}
+
+// Cluster batch: 16 equations per thread, nt in {64, 128, 256} threads per
+// CTA, P = n / (16 nt) CTAs per system with P in {2, 4, 8, 16}.
+int launch_batch_cl(const BatchArgs &A, const TileConfig &cfg, cudaStream_t st) {
+    if (A.residual == TPRGB_RESID_F64 && A.refine_steps > 0)
+        return fail(TPRGB_EUNSUPPORTED, "cluster kernel has no FP64 residual mode");
+    int P = 0;
+    int rc = cluster_parts(A.n, cfg, &P);
+    if (rc) return rc;
+    if (A.nsys == 0) return TPRGB_OK;
+    if (cfg.nt == 64) return launch_cl_mode<64>(A, P, st);
+    return cfg.nt == 128 ? launch_cl_mode<128>(A, P, st) : launch_cl_mode<256>(A, P, st);
+}
+
+int cluster_parts(int n, const TileConfig &cfg, int *P) {
+    if (cfg.L != 16 || (cfg.nt != 64 && cfg.nt != 128 && cfg.nt != 256))
+        return fail(TPRGB_EINVAL, "cluster tiles use 16 equations per thread and 64, "
+                                  "128 or 256 threads");
+    if (!is_pow2(n) || n < 2 * 16 * cfg.nt || n > 16 * 16 * cfg.nt)
+        return fail(TPRGB_EINVAL, "n=%d needs 2..16 CTAs of %d equations", n, 16 * cfg.nt);
+    *P = n / (16 * cfg.nt);
+    return TPRGB_OK;
 }
 
 int sw_status(unsigned (&v)[4], bool reset) {

@@ -4,6 +4,7 @@
 // (then the CTAs exchange their boundary rows through global scratch).
 #pragma once
 
+#include "cluster.cuh"
 #include "common.cuh"
 #include "hier.cuh"
 
@@ -27,10 +28,14 @@ struct Smem {
     float4 edge[2 * (NT / 32)];
     float2 part_nb;  // previous part's last / next part's first unknown
     int ok;
+    float4 crow[2][2];  // cluster parts: this CTA's two boundary rows per parity
 };
 
-// Multi-CTA system context.  Scratch per system: counter, then rows
-// [2 parity][32 parts][8 floats] and edges [2 parity][32 parts][4 floats].
+// Multi-CTA system context.  on = 1: the parts are CTAs of a persistent
+// grid meeting at counter barriers in global scratch (per system: counter,
+// then rows [2 parity][32 parts][8 floats] and edges [2 parity][32 parts][4
+// floats]); on = 2: the parts are the CTAs of one thread-block cluster,
+// exchanging rows through distributed shared memory at cluster barriers.
 struct Part {
     int on, P, p;
     unsigned *counter;
@@ -142,26 +147,44 @@ __device__ __forceinline__ void solve(const float (&a)[L], const float (&b)[L],
                 }
                 hier::seg_reduce_k<W>(S0, S1, q2);
             }
-            // level 3: this CTA's two boundary rows -> scratch, barrier,
-            // every part solves the 2P-row system redundantly
+            // level 3: this CTA's two boundary rows -> scratch (global
+            // memory, or this CTA's shared memory for cluster parts),
+            // barrier, every part solves the 2P-row system redundantly
             const unsigned par = pc.round & 1u;
-            if (warp == 0 && lane == 0) {
-                float4 *dst = reinterpret_cast<float4 *>(pc.rows + (par * 32 + pc.p) * 8);
-                __stcg(dst, make_float4(S0.a, S0.c, S0.d, 0.f));
-                writer_fence();
+            if (pc.on == 2) {
+                if (warp == 0 && lane == 0)
+                    sm.crow[par][0] = make_float4(S0.a, S0.c, S0.d, 0.f);
+                if (warp == 0 && lane == W - 1)
+                    sm.crow[par][1] = make_float4(S1.a, S1.c, S1.d, 0.f);
+                cl::sync();
+                pc.round++;
+            } else {
+                if (warp == 0 && lane == 0) {
+                    float4 *dst = reinterpret_cast<float4 *>(pc.rows + (par * 32 + pc.p) * 8);
+                    __stcg(dst, make_float4(S0.a, S0.c, S0.d, 0.f));
+                    writer_fence();
+                }
+                if (warp == 0 && lane == W - 1) {
+                    float4 *dst = reinterpret_cast<float4 *>(pc.rows + (par * 32 + pc.p) * 8 + 4);
+                    __stcg(dst, make_float4(S1.a, S1.c, S1.d, 0.f));
+                    writer_fence();
+                }
+                part_barrier<NT>(pc, sm, 1);
             }
-            if (warp == 0 && lane == W - 1) {
-                float4 *dst = reinterpret_cast<float4 *>(pc.rows + (par * 32 + pc.p) * 8 + 4);
-                __stcg(dst, make_float4(S1.a, S1.c, S1.d, 0.f));
-                writer_fence();
-            }
-            part_barrier<NT>(pc, sm, 1);
             if (warp == 0) {
                 const int P = pc.P;
                 Row U0{0.f, 0.f, 0.f}, U1{0.f, 0.f, 0.f};
                 if (lane < P) {
-                    const float4 *src = reinterpret_cast<const float4 *>(pc.rows + (par * 32 + lane) * 8);
-                    float4 v0 = __ldcg(src), v1 = __ldcg(src + 1);
+                    float4 v0, v1;
+                    if (pc.on == 2) {
+                        const uint32_t ra = cl::map(&sm.crow[par][0], (unsigned)lane);
+                        v0 = cl::ld4(ra);
+                        v1 = cl::ld4(ra + 16u);
+                    } else {
+                        const float4 *src = reinterpret_cast<const float4 *>(pc.rows + (par * 32 + lane) * 8);
+                        v0 = __ldcg(src);
+                        v1 = __ldcg(src + 1);
+                    }
                     U0 = Row{v0.x, v0.y, v0.z};
                     U1 = Row{v1.x, v1.y, v1.z};
                 }
@@ -259,6 +282,33 @@ __device__ __forceinline__ void neighbours(float hfirst, float hlast,
     }
 }
 
+// Residuals of a chunk's rows for x = xh + xlo (hm/lm, hp/lp: the
+// neighbouring unknowns outside the chunk).  lo_terms = false in the first
+// refinement step, where xlo is zero: one uniform branch per chunk picks
+// the form without the lo products.
+template <int L>
+__device__ __forceinline__ void residuals(const float (&a)[L], const float (&b)[L],
+                                          const float (&c)[L], const float (&d)[L],
+                                          const float (&xh)[L], const float (&xlo)[L],
+                                          float hm, float lm, float hp, float lp,
+                                          bool lo_terms, float (&r)[L]) {
+    if (lo_terms) {
+#pragma unroll
+        for (int i = 0; i < L; i++)
+            r[i] = hier::residual_df<true>(a[i], b[i], c[i], d[i],
+                                           i > 0 ? xh[i - 1] : hm,
+                                           i > 0 ? xlo[i - 1] : lm, xh[i], xlo[i],
+                                           i < L - 1 ? xh[i + 1] : hp,
+                                           i < L - 1 ? xlo[i + 1] : lp);
+    } else {
+#pragma unroll
+        for (int i = 0; i < L; i++)
+            r[i] = hier::residual_df<false>(a[i], b[i], c[i], d[i],
+                                            i > 0 ? xh[i - 1] : hm, 0.f, xh[i], 0.f,
+                                            i < L - 1 ? xh[i + 1] : hp, 0.f);
+    }
+}
+
 template <int L>
 __device__ __forceinline__ void load_chunk(const float *__restrict__ p,
                                            float (&v)[L]) {
@@ -318,15 +368,7 @@ __device__ __forceinline__ bool run_tile(
             if (MODE == 1) {
                 neighbours<NT, T>(xh[0], xh[L - 1], xlo[0], xlo[L - 1], t, hm,
                                   lm, hp, lp, sm, pc);
-#pragma unroll
-                for (int i = 0; i < L; i++) {
-                    float xmh = i > 0 ? xh[i - 1] : hm;
-                    float xml = i > 0 ? xlo[i - 1] : lm;
-                    float xph = i < L - 1 ? xh[i + 1] : hp;
-                    float xpl = i < L - 1 ? xlo[i + 1] : lp;
-                    r[i] = hier::residual_df(a[i], b[i], c[i], d[i], xmh, xml,
-                                             xh[i], xlo[i], xph, xpl);
-                }
+                residuals<L>(a, b, c, d, xh, xlo, hm, lm, hp, lp, step > 0, r);
             } else {
                 float fh = (float)xd[0], fl = (float)(xd[0] - (double)fh);
                 float lh = (float)xd[L - 1], ll = (float)(xd[L - 1] - (double)lh);
@@ -358,20 +400,14 @@ __device__ __forceinline__ bool run_tile(
 
     bool finite = true;
     if (!active) return true;
-    if (x_f64) {
+    if (x_f64 && MODE != 2) {
+        finite = hier::store_pairs_f64<L>(xh, xlo, (double *)gx + base);
+    } else if (x_f64) {
         double2 *o = reinterpret_cast<double2 *>((double *)gx + base);
 #pragma unroll
         for (int i = 0; i < L / 2; i++) {
-            double v0, v1;
-            if (MODE == 2) {
-                v0 = xd[2 * i];
-                v1 = xd[2 * i + 1];
-            } else {
-                v0 = hier::pair_to_double(xh[2 * i], xlo[2 * i]);
-                v1 = hier::pair_to_double(xh[2 * i + 1], xlo[2 * i + 1]);
-            }
             finite = finite && isfinite(xh[2 * i]) && isfinite(xh[2 * i + 1]);
-            o[i] = make_double2(v0, v1);
+            o[i] = make_double2(xd[2 * i], xd[2 * i + 1]);
         }
     } else {
         float4 *o = reinterpret_cast<float4 *>((float *)gx + base);
@@ -492,15 +528,7 @@ __device__ __forceinline__ bool run_tile_smem(
             {
                 float a[L], b[L], c[L], d[L];
                 load4(a, b, c, d);
-#pragma unroll
-                for (int i = 0; i < L; i++) {
-                    float xmh = i > 0 ? xh[i - 1] : hm;
-                    float xml = i > 0 ? xlo[i - 1] : lm;
-                    float xph = i < L - 1 ? xh[i + 1] : hp;
-                    float xpl = i < L - 1 ? xlo[i + 1] : lp;
-                    r[i] = hier::residual_df(a[i], b[i], c[i], d[i], xmh, xml,
-                                             xh[i], xlo[i], xph, xpl);
-                }
+                residuals<L>(a, b, c, d, xh, xlo, hm, lm, hp, lp, step > 0, r);
             }
             float dx[L];
             {
@@ -515,14 +543,7 @@ __device__ __forceinline__ bool run_tile_smem(
     bool finite = true;
     if (!active) return true;
     if (x_f64) {
-        double2 *o = reinterpret_cast<double2 *>((double *)gx + base);
-#pragma unroll
-        for (int i = 0; i < L / 2; i++) {
-            double v0 = hier::pair_to_double(xh[2 * i], xlo[2 * i]);
-            double v1 = hier::pair_to_double(xh[2 * i + 1], xlo[2 * i + 1]);
-            finite = finite && isfinite(xh[2 * i]) && isfinite(xh[2 * i + 1]);
-            o[i] = make_double2(v0, v1);
-        }
+        finite = hier::store_pairs_f64<L>(xh, xlo, (double *)gx + base);
     } else {
         float4 *o = reinterpret_cast<float4 *>((float *)gx + base);
 #pragma unroll

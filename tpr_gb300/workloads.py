@@ -226,10 +226,28 @@ def precision(nsys=1024, n=32768, steps=2):
     w64, _ = port.batch_rel_l2(bt, x64h, truth)
     wvs, _ = port.batch_rel_l2(bt, x.cpu().numpy(), x64h)
     gbs = 24 * bt.neq / t / 1e9
+    # the same systems through the uniform batch API (all share n): one
+    # thread-block cluster per system
+    xb = torch.empty(bt.neq, dtype=torch.float64, device="cuda")
+    o = B.opts(refine_steps=steps)
+    for _ in range(2):
+        B.solve_into(xb, *dev, n, o)
+    s0.record()
+    for _ in range(reps):
+        B.solve_into(xb, *dev, n, o)
+    s1.record()
+    torch.cuda.synchronize()
+    tb = s0.elapsed_time(s1) * 1e-3 / reps
+    wb, _ = port.batch_rel_l2(bt, xb.cpu().numpy(), truth)
+    gbb = 24 * bt.neq / tb / 1e9
     return {"workload": f"precision stress {nsys} x N={n}, weakly dominant, "
                         f"FP32 + {steps} refinement steps",
             "systems_per_s": nsys / t, "gb_per_s": gbs,
             "frac_of_peak": gbs / _peak(), "rel_l2_max_vs_thomas": worst,
+            "uniform_batch_api": {"systems_per_s": nsys / tb, "gb_per_s": gbb,
+                                  "frac_of_peak": gbb / _peak(),
+                                  "rel_l2_max_vs_thomas": wb,
+                                  "tile": list(B.tile_for(n))},
             "plain_fp64_gpu": {"systems_per_s": nsys / t64,
                                "rel_l2_max_vs_thomas": w64},
             "rel_l2_max_vs_plain_fp64_gpu": wvs}
