@@ -237,12 +237,16 @@ TPRGB_API int tprgb_tune_clear(void);
 
 /* ---- uneven batches: plan + persistent queue kernel ---------------------
  * A plan fixes the sizes and offsets of a batch of systems (any mix of
- * power-of-two n, 16 <= n <= 32 * CTA tile); tprgb_plan_execute solves
- * them in one cooperative launch of a persistent kernel whose CTAs pull
- * work items (largest systems first) from a device queue.  Systems larger
- * than one CTA's tile are split over several CTAs that exchange their
- * reduced rows through the plan's scratch with bounded waits.  Replaces
- * the reference's one-launch-per-system loop (src/pm.cpp:224-238). */
+ * power-of-two n, 16 <= n <= 32 * CTA tile) and routes them by size:
+ * systems of 256..4096 equations whose offsets are multiples of 32 go to
+ * the swizzled staged kernel (one launch per size, per-system offsets),
+ * 8192..65536 to the thread-block cluster kernel; the rest to one
+ * cooperative launch of a persistent kernel whose CTAs pull work items
+ * (largest systems first) from a device queue, systems larger than one
+ * CTA's tile split over CTAs that exchange their reduced rows through the
+ * plan's scratch with bounded waits.  opts->variant = 1 or the FP64
+ * residual keeps every system on the queue kernel.  Replaces the
+ * reference's one-launch-per-system loop (src/pm.cpp:224-238). */
 typedef struct tprgb_plan tprgb_plan;
 
 /* offsets[k]: first element of system k in every array (multiple of 4);
@@ -264,6 +268,11 @@ TPRGB_API int tprgb_plan_execute(tprgb_plan *plan, const float *d_a,
 
 TPRGB_API int tprgb_plan_info(const tprgb_plan *plan, int *nitems, int *grid,
                               int *nlarge, int *graph_active);
+
+/* Systems on each route and the launches one execute makes. */
+TPRGB_API int tprgb_plan_routes(const tprgb_plan *plan, int *staged_systems,
+                                int *cluster_systems, int *queue_systems,
+                                int *launches);
 
 /* After an execute on `stream` (waits for it): sys_status[k] (may be NULL)
  * is 0 or 1 (non-finite solution) per system in the caller's order;
@@ -308,6 +317,11 @@ typedef struct tprgb_server_opts {
                             overlaps building the next step with the running
                             one; 1 makes an arrival wait for at most the
                             running step                                    */
+    int kernel_routes;   /* 1 (default): a step's size groups of 256..4096
+                            equations go to the staged kernel and of
+                            8192..65536 to the cluster kernel, one launch
+                            per size, the rest to the queue kernel; 0: the
+                            whole step on the queue kernel                 */
 } tprgb_server_opts;
 
 typedef struct tprgb_request_info {

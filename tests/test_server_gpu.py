@@ -163,3 +163,24 @@ def test_one_step_in_flight_same_bits(cuda):
     with pytest.raises(T.TprError) as e:
         Server(budget_bytes=1 << 24, max_inflight=3)
     assert e.value.code == T.EINVAL
+
+
+def test_routed_and_queue_only_steps(cuda, port):
+    """Steps whose size groups go to the staged / cluster kernels and steps
+    kept on the queue kernel both meet 1e-9 against FP64 Thomas."""
+    rng = np.random.default_rng(33)
+    reqs = [_req(rng, 8, 8, 14) for _ in range(6)]
+    out = {}
+    for routes in (True, False):
+        with Server(budget_bytes=1 << 30, kernel_routes=routes) as s:
+            ts = [s.submit_seeded(*r) for r in reqs]
+            infos = [s.wait(t) for t in ts]
+            assert all(i["rc"] == 0 for i in infos)
+            out[routes] = [(s.fetch(t, int(r[0].sum())),
+                            s.fetch_system(t, int(r[0].sum())))
+                           for t, r in zip(ts, reqs)]
+    for routes in (True, False):
+        for (x, (a, b, c, d)), r in zip(out[routes], reqs):
+            bt = G.Batch(r[0], a, b, c, d, np.zeros(len(a)))
+            worst, _ = port.batch_rel_l2(bt, x, port.batch_thomas(bt))
+            assert worst <= 1e-9, (routes, worst)

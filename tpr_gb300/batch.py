@@ -46,6 +46,8 @@ def _declare(L):
         "tprgb_plan_execute": (i, [vp, vp, vp, vp, vp, vp, vp]),
         "tprgb_plan_info": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i),
                                 C.POINTER(i)]),
+        "tprgb_plan_routes": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i),
+                                  C.POINTER(i)]),
         "tprgb_plan_status": (i, [vp, vp, C.POINTER(C.c_uint), vp]),
     }
     for name, (res, args) in sig.items():
@@ -147,12 +149,15 @@ class HostContext:
 
 
 class Plan:
-    """Uneven batch: systems of any power-of-two sizes at given offsets,
-    solved by the persistent queue kernel (tprgb_plan_*)."""
+    """Uneven batch: systems of any power-of-two sizes at given offsets
+    (tprgb_plan_*), routed by size to the staged, cluster or persistent
+    queue kernels; variant=REGISTERS keeps every system on the queue
+    kernel."""
 
     def __init__(self, ns, offsets=None, refine_steps: int = 1,
                  residual: int = RESID_DF, x_f64: bool = True,
-                 threads_per_cta: int = 0, graph: bool = True):
+                 threads_per_cta: int = 0, graph: bool = True,
+                 variant: int = 0):
         ns = np.ascontiguousarray(ns, np.int32)
         if offsets is None:
             offsets = np.zeros(len(ns), np.int64)
@@ -162,7 +167,7 @@ class Plan:
         self.ns, self.offsets = ns, offsets
         self.neq = int((offsets + ns).max()) if len(ns) else 0
         self.x_f64 = x_f64
-        o = opts(refine_steps, residual, x_f64, 0, threads_per_cta)
+        o = opts(refine_steps, residual, x_f64, 0, threads_per_cta, variant)
         self._h = C.c_void_p()
         check(load().tprgb_plan_create(len(ns), offsets.ctypes.data,
                                        ns.ctypes.data, C.byref(o),
@@ -180,8 +185,13 @@ class Plan:
     def info(self):
         v = [C.c_int() for _ in range(4)]
         check(load().tprgb_plan_info(self._h, *[C.byref(t) for t in v]))
-        return dict(zip(("items", "grid", "multi_cta_systems", "graph"),
-                        [t.value for t in v]))
+        out = dict(zip(("items", "grid", "multi_cta_systems", "graph"),
+                       [t.value for t in v]))
+        r = [C.c_int() for _ in range(4)]
+        check(load().tprgb_plan_routes(self._h, *[C.byref(t) for t in r]))
+        out.update(zip(("staged_systems", "cluster_systems", "queue_systems",
+                        "launches"), [t.value for t in r]))
+        return out
 
     def status(self, stream=None):
         """(rc, per-system status array, device code) after an execute."""
@@ -208,12 +218,15 @@ class Plan:
 
 def solve_plan_host(batch, refine_steps: int = 1, residual: int = RESID_DF,
                     x_f64: bool = True, threads_per_cta: int = 0,
-                    graph: bool = False, repeats: int = 1):
+                    graph: bool = False, repeats: int = 1, variant: int = 0,
+                    info: dict | None = None):
     """Solve a generate.Batch (any sizes) through a plan; returns (x, plan
-    status tuple)."""
+    status tuple); `info` (a dict) receives the plan's info()."""
     torch = _torch()
     p = Plan(batch.ns, batch.offsets, refine_steps, residual, x_f64,
-             threads_per_cta, graph)
+             threads_per_cta, graph, variant)
+    if info is not None:
+        info.update(p.info())
     dev = [torch.from_numpy(v).cuda() for v in (batch.a, batch.b, batch.c,
                                                   batch.d)]
     x = torch.empty(batch.neq, dtype=torch.float64 if x_f64 else

@@ -38,6 +38,14 @@ int launch_batch_uniform(const BatchArgs &A, const TileConfig &cfg,
 int launch_batch_tma(const BatchArgs &A, const TileConfig &cfg, cudaStream_t st);
 int launch_batch_sw(const BatchArgs &A, const TileConfig &cfg, cudaStream_t st);
 int launch_batch_cl(const BatchArgs &A, const TileConfig &cfg, cudaStream_t st);
+
+// A size group of a plan solved by the staged (kind 1) or cluster (kind 2)
+// kernel: sorted systems [first, first + count) of size n.
+struct Route {
+    int kind = 0;
+    int n = 0, first = 0, count = 0;
+    TileConfig cfg{16, 64, 3};
+};
 // CTAs per system of the cluster variant for size n (error if invalid)
 int cluster_parts(int n, const TileConfig &cfg, int *P);
 // status word of the swizzled kernels (code, where, tile); reset clears it

@@ -140,6 +140,8 @@ plan_persistent(const float *__restrict__ ga, const float *__restrict__ gb,
 
 struct Plan {
     int nsys = 0, nitems = 0, nlarge = 0;
+    std::vector<Route> routes;  // size groups on the staged / cluster kernels
+    long long total_eq = 0;     // extent of the arrays the systems cover
     int nt = 256, refine_steps = 1, residual = TPRGB_RESID_DF, x_f64 = 1;
     int grid = 0;
     std::vector<int> order;  // sorted position -> caller's system index
@@ -174,13 +176,41 @@ static const void *plan_kernel(int nt, int mode) {
     return plan_kernel_ptr<512, 2>();
 }
 
+// Staged or cluster kernel for the sorted systems [k, e) of size n, if one
+// serves them: offsets multiples of 32 equations (rows of the tensor-map
+// loads), 256 <= n <= 4096 (one CTA per system, swizzled staging) or
+// 8192 <= n <= 65536 (one thread-block cluster per system).
+static bool route_for(int n, const std::vector<long long> &off, int k, int e,
+                      Route &r) {
+    for (int i = k; i < e; i++)
+        if (off[i] & 31) return false;
+    TileConfig c = tuned_tile(n);
+    if (n >= 256 && n <= 4096) {
+        const bool sw = (c.staged == 2 || c.staged == 3) && (c.L == 8 || c.L == 16) &&
+                        (c.nt == 64 || c.nt == 128 || c.nt == 256) && n / c.L <= c.nt;
+        if (!sw) c = TileConfig{16, std::max(64, n / 16), 3};
+        r = Route{1, n, k, e - k, c};
+        return true;
+    }
+    if (n >= 8192 && n <= 65536) {
+        if (c.staged != 4) c = TileConfig{16, 256, 4};
+        const int P = n / (16 * c.nt);
+        if (n % (16 * c.nt) || P < 2 || P > 16) return false;
+        r = Route{2, n, k, e - k, c};
+        return true;
+    }
+    return false;
+}
+
 // Work items for a batch: systems sorted by decreasing n (order[k] = the
 // caller's index of sorted system k, off[k] its offset); small systems
 // packed per CTA, larger ones split into P parts (slot = multi-CTA
-// systems so far, incremented).
+// systems so far, incremented).  With `routes`, size groups that a staged
+// or cluster kernel serves are listed there instead of becoming items.
 int build_items(int nsys, const int64_t *offsets, const int *ns, int nt,
                 std::vector<int> &order, std::vector<int4> &items,
-                std::vector<long long> &off, int &slot) {
+                std::vector<long long> &off, int &slot,
+                std::vector<Route> *routes) {
     order.resize(nsys);
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(),
@@ -193,6 +223,12 @@ int build_items(int nsys, const int64_t *offsets, const int *ns, int nt,
         const int n = ns[order[k]];
         int e = k;
         while (e < nsys && ns[order[e]] == n) e++;
+        Route r;
+        if (routes && route_for(n, off, k, e, r)) {
+            routes->push_back(r);
+            k = e;
+            continue;
+        }
         TileConfig tc = tuned_tile(n);
         int L = tc.L == 4 ? 4 : 8;
         if (n < 2 * L) L = 4;
@@ -299,7 +335,14 @@ int plan_create(int nsys, const int64_t *offsets, const int *ns,
     std::vector<int4> items;
     std::vector<long long> off;
     int slot = 0;
-    int rc = build_items(nsys, offsets, ns, nt, p->order, items, off, slot);
+    // staged / cluster routes unless the caller asks for the register
+    // kernel (variant 1) or the FP64 residual (queue kernel only)
+    const bool use_routes = o.variant != 1 &&
+                            !(o.residual == TPRGB_RESID_F64 && o.refine_steps > 0);
+    int rc = build_items(nsys, offsets, ns, nt, p->order, items, off, slot,
+                         use_routes ? &p->routes : nullptr);
+    for (int k = 0; k < nsys; k++)
+        p->total_eq = std::max<long long>(p->total_eq, offsets[k] + ns[k]);
     if (rc) {
         plan_free(p);
         return rc;
@@ -317,7 +360,7 @@ int plan_create(int nsys, const int64_t *offsets, const int *ns,
         plan_free(p);
         return fail(TPRGB_EUNSUPPORTED, "only %d resident CTAs", resident);
     }
-    p->grid = std::max(1, std::min(resident, p->nitems));
+    p->grid = std::max(1, std::min(resident, std::max(p->nitems, 1)));
 
     p->ctl_words = 16 + (size_t)p->nlarge + (size_t)nsys;
     std::vector<unsigned> ctl_init(16, 0u);
@@ -354,10 +397,22 @@ static int plan_reset(Plan *p, cudaStream_t st) {
     return TPRGB_OK;
 }
 
+// One launch per routed size group (largest first), then the queue kernel
+// for the remaining systems.
 static int plan_launch(Plan *p, const float *a, const float *b, const float *c,
                        const float *d, void *x, cudaStream_t st) {
     int rc = plan_reset(p, st);
     if (rc) return rc;
+    unsigned *sys_status = p->d_ctl + 16 + p->nlarge;
+    for (const Route &r : p->routes) {
+        BatchArgs A{a, b, c, d, x, r.count, r.n, p->refine_steps, p->residual, p->x_f64};
+        A.sys_off = p->d_off + r.first;
+        A.sys_status = sys_status + r.first;
+        A.status = p->d_ctl + 4;
+        A.total_eq = p->total_eq;
+        rc = r.kind == 2 ? launch_batch_cl(A, r.cfg, st) : launch_batch_sw(A, r.cfg, st);
+        if (rc) return rc;
+    }
     return launch_persistent(p->nt, plan_mode(*p), p->grid, a, b, c, d, x,
                              p->d_items, p->nitems, p->d_off, p->d_ctl,
                              p->d_scratch, p->refine_steps, p->x_f64, st);
@@ -465,6 +520,20 @@ TPRGB_API int tprgb_plan_info(const tprgb_plan *plan, int *nitems, int *grid,
     if (grid) *grid = plan->p->grid;
     if (nlarge) *nlarge = plan->p->nlarge;
     if (graph_active) *graph_active = plan->p->gexec != nullptr;
+    return TPRGB_OK;
+}
+
+TPRGB_API int tprgb_plan_routes(const tprgb_plan *plan, int *staged_systems,
+                                int *cluster_systems, int *queue_systems,
+                                int *launches) {
+    if (!plan) return fail(TPRGB_EINVAL, "plan is NULL");
+    const Plan *p = plan->p;
+    int st = 0, clu = 0;
+    for (const Route &r : p->routes) (r.kind == 2 ? clu : st) += r.count;
+    if (staged_systems) *staged_systems = st;
+    if (cluster_systems) *cluster_systems = clu;
+    if (queue_systems) *queue_systems = p->nsys - st - clu;
+    if (launches) *launches = (int)p->routes.size() + (p->nitems > 0 ? 1 : 0);
     return TPRGB_OK;
 }
 

@@ -36,7 +36,8 @@ namespace tprgb {
 // plan_kernels.cu / gen_kernels.cu
 int build_items(int nsys, const int64_t *offsets, const int *ns, int nt,
                 std::vector<int> &order, std::vector<int4> &items,
-                std::vector<long long> &off, int &slot);
+                std::vector<long long> &off, int &slot,
+                std::vector<Route> *routes);
 int persistent_capacity(int nt, int mode, int *resident);
 int launch_persistent(int nt, int mode, int grid, const float *a,
                       const float *b, const float *c, const float *d, void *x,
@@ -53,8 +54,10 @@ using Clock = std::chrono::steady_clock;
 class RangeAlloc {
    public:
     explicit RangeAlloc(long long cap) : cap_(cap) { free_[0] = cap; }
+    // ranges start at multiples of 32 equations (128-byte rows of the
+    // staged kernels' tensor-map loads)
     long long alloc(long long n) {
-        n = (n + 3) & ~3LL;
+        n = (n + 31) & ~31LL;
         for (auto it = free_.begin(); it != free_.end(); ++it) {
             if (it->second >= n) {
                 long long at = it->first, rest = it->second - n;
@@ -67,7 +70,7 @@ class RangeAlloc {
         return -1;
     }
     void release(long long at, long long n) {
-        n = (n + 3) & ~3LL;
+        n = (n + 31) & ~31LL;
         used_ -= n;
         auto it = free_.emplace(at, n).first;
         auto nx = std::next(it);
@@ -326,8 +329,10 @@ static int launch_step(Server *s) {
     std::vector<int4> items;
     std::vector<long long> soff;
     int nlarge = 0;
+    std::vector<Route> routes;
+    const bool use_routes = s->o.kernel_routes && s->mode != 2;
     int rc = build_items(st.nsys, off.data(), ns.data(), s->o.threads_per_cta,
-                         st.order, items, soff, nlarge);
+                         st.order, items, soff, nlarge, use_routes ? &routes : nullptr);
     if (rc) return rc;
     // both buffers alternate; a buffer is reused two steps later, after the
     // step that used it completed (at most two steps in flight)
@@ -352,6 +357,18 @@ static int launch_step(Server *s) {
                                cudaMemcpyHostToDevice, cs));
     TPRGB_CUDA(cudaMemcpyAsync(b.ctl, b.h_ctl, sizeof(unsigned) * ctl_words,
                                cudaMemcpyHostToDevice, cs));
+    // size groups on the staged / cluster kernels (largest first), the
+    // rest on the queue kernel
+    for (const Route &r : routes) {
+        BatchArgs A{s->A, s->B, s->Cc, s->D, s->X, r.count, r.n, s->o.refine_steps,
+                    s->o.residual, 1};
+        A.sys_off = b.off + r.first;
+        A.sys_status = b.ctl + 16 + nlarge + r.first;
+        A.status = b.ctl + 4;
+        A.total_eq = s->cap_eq;
+        rc = r.kind == 2 ? launch_batch_cl(A, r.cfg, cs) : launch_batch_sw(A, r.cfg, cs);
+        if (rc) return rc;
+    }
     int grid = std::max(1, std::min(s->grid, (int)items.size()));
     rc = launch_persistent(s->o.threads_per_cta, s->mode, grid, s->A, s->B,
                            s->Cc, s->D, s->X, b.items, (int)items.size(), b.off,
@@ -568,6 +585,7 @@ TPRGB_API int tprgb_server_opts_default(tprgb_server_opts *o) {
     o->threads_per_cta = 256;
     o->max_step_eq = 0;
     o->max_inflight = 2;
+    o->kernel_routes = 1;
     return TPRGB_OK;
 }
 
@@ -589,7 +607,7 @@ TPRGB_API int tprgb_server_create(const tprgb_server_opts *opts,
         return fail(TPRGB_EINVAL, "max_inflight must be 1 or 2");
     }
     s->mode = s->o.refine_steps <= 0 ? 0 : (s->o.residual == TPRGB_RESID_F64 ? 2 : 1);
-    s->cap_eq = (long long)(s->o.budget_bytes / 24) & ~3LL;
+    s->cap_eq = (long long)(s->o.budget_bytes / 24) & ~31LL;
     if (s->cap_eq < 1024) {
         delete s;
         return fail(TPRGB_EINVAL, "budget too small");

@@ -22,14 +22,17 @@ from .server import Server
 
 def run(nreq: int, budget_gib: float = 8.0, loads=(0.25, 0.5, 0.9),
         seed: int = 11, max_sys: int = 512, max_step_eq: int = 0,
-        max_inflight: int = 2):
+        max_inflight: int = 2, kernel_routes: bool = True):
     out = {"workload": f"{nreq} requests, U{{1..{max_sys}}} systems of "
                        f"N=2^U{{8..14}}, FP32 + 1 refinement, "
                        f"{budget_gib:g} GiB budget, step cap "
                        f"{max_step_eq or 'none'} eq, {max_inflight} step(s) "
-                       f"in flight", "loads": []}
+                       f"in flight, "
+                       f"{'size routes' if kernel_routes else 'queue kernel only'}",
+           "loads": []}
     with Server(budget_bytes=int(budget_gib * (1 << 30)),
-                max_step_eq=max_step_eq, max_inflight=max_inflight) as s:
+                max_step_eq=max_step_eq, max_inflight=max_inflight,
+                kernel_routes=kernel_routes) as s:
         s.run_load(min(nreq, 64), 0.0, seed=seed + 99, max_sys=max_sys)  # warm
         lat, el, nsys, rc = s.run_load(nreq, 0.0, seed=seed, max_sys=max_sys)
         sat_req = nreq / el
@@ -66,12 +69,15 @@ def main():
     p.add_argument("--budget-gib", type=float, default=8.0)
     p.add_argument("--max-step-eq", type=int, default=0)
     p.add_argument("--max-inflight", type=int, default=2, choices=(1, 2))
+    p.add_argument("--queue-only", action="store_true",
+                   help="every step on the persistent queue kernel")
     a = p.parse_args()
     from . import autotune
     autotune.apply()
     print(json.dumps(run(a.requests, a.budget_gib,
                          max_step_eq=a.max_step_eq,
-                         max_inflight=a.max_inflight)), flush=True)
+                         max_inflight=a.max_inflight,
+                         kernel_routes=not a.queue_only)), flush=True)
 
 
 if __name__ == "__main__":

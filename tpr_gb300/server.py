@@ -20,7 +20,7 @@ class ServerOpts(C.Structure):
     _fields_ = [("budget_bytes", C.c_size_t), ("max_pending", C.c_int),
                 ("refine_steps", C.c_int), ("residual", C.c_int),
                 ("threads_per_cta", C.c_int), ("max_step_eq", C.c_longlong),
-                ("max_inflight", C.c_int)]
+                ("max_inflight", C.c_int), ("kernel_routes", C.c_int)]
 
 
 class RequestInfo(C.Structure):
@@ -66,7 +66,7 @@ class Server:
     def __init__(self, budget_bytes: int = 8 << 30, refine_steps: int = 1,
                  residual: int = 0, threads_per_cta: int = 256,
                  max_pending: int = 1 << 20, max_step_eq: int = 0,
-                 max_inflight: int = 2):
+                 max_inflight: int = 2, kernel_routes: bool = True):
         L = load()
         _declare(L)
         o = ServerOpts()
@@ -78,6 +78,7 @@ class Server:
         o.max_pending = max_pending
         o.max_step_eq = max_step_eq
         o.max_inflight = max_inflight
+        o.kernel_routes = int(bool(kernel_routes))
         self._h = C.c_void_p()
         self._keep = {}
         check(L.tprgb_server_create(C.byref(o), C.byref(self._h)))
