@@ -186,11 +186,6 @@ batch_cl(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
     __syncthreads();
     auto issue = [&](long long sys) {  // thread 0 only
         tma::fence_proxy_async();
-        if (sys + nclusters < nsys) {  // this CTA's next part, into L2
-            const int row = (int)((sys_base(sys + nclusters) >> 5) + (long long)p * ROWS);
-#pragma unroll
-            for (int k = 0; k < 4; k++) tma::tensor_prefetch_2d(&tm.m[k], 0, row);
-        }
         tma::mbar_expect_tx(&full, 4u * TILE * 4u);
 #pragma unroll
         for (int k = 0; k < 4; k++)

@@ -58,14 +58,6 @@ __device__ __forceinline__ void tensor_g2s_2d(void *dst, const void *tmap,
         : "memory");
 }
 
-// Prefetch one box of a 2D tensor map into L2 (no shared memory, no
-// completion to wait for).
-__device__ __forceinline__ void tensor_prefetch_2d(const void *tmap, int x, int y) {
-    asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"(tmap),
-                 "r"(x), "r"(y)
-                 : "memory");
-}
-
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned phase) {
     uint32_t ok;
     asm volatile(
