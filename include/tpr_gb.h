@@ -209,8 +209,10 @@ TPRGB_API int tprgb_batch_solve(int nsys, int n, const float *d_a,
 /* ---- host-buffer batched solve (pinned host arrays, e.g. for callers that
  * keep systems on the host; the counterpart of the reference wrappers'
  * H2D -> launch -> D2H sequence, src/ptpr.cu:542-600, without per-call
- * allocation).  The batch is cut into chunks; chunk k+1's upload overlaps
- * chunk k's solve and chunk k-1's download on two streams. ------------- */
+ * allocation).  The batch is cut into chunks rotating over three streams;
+ * chunk k+1's upload overlaps chunk k's solve and the downloads of earlier
+ * chunks.  Bound by the host link (GB300 machine measured: 209 GB/s up, 192
+ * GB/s down, 277 GB/s both ways at once). ---------------------------- */
 typedef struct tprgb_host_ctx tprgb_host_ctx;
 
 /* Device buffers for chunks of up to chunk_eq equations (two in flight). */

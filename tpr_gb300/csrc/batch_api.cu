@@ -131,16 +131,22 @@ TPRGB_API int tprgb_batch_solve(int nsys, int n, const float *d_a,
 }  // extern "C"
 
 // ---- host-buffer pipeline -------------------------------------------------
+// Chunks rotate over kHostStreams streams, each with its own device buffers:
+// a chunk's upload waits only for the download of the chunk kHostStreams
+// earlier, so the host-to-device link stays busy while the previous chunks
+// solve and download.
+constexpr int kHostStreams = 3;
+
 struct tprgb_host_ctx {
     int64_t chunk_eq = 0;
-    cudaStream_t st[2] = {nullptr, nullptr};
-    cudaEvent_t up[2] = {nullptr, nullptr};
-    float *d_in[2] = {nullptr, nullptr};  // a, b, c, d of one chunk
-    void *d_x[2] = {nullptr, nullptr};    // x of one chunk (8 B / eq)
+    cudaStream_t st[kHostStreams] = {};
+    cudaEvent_t up[kHostStreams] = {};
+    float *d_in[kHostStreams] = {};  // a, b, c, d of one chunk
+    void *d_x[kHostStreams] = {};    // x of one chunk (8 B / eq)
 };
 
 static void host_ctx_free(tprgb_host_ctx *h) {
-    for (int i = 0; i < 2; i++) {
+    for (int i = 0; i < kHostStreams; i++) {
         if (h->st[i]) cudaStreamDestroy(h->st[i]);
         if (h->up[i]) cudaEventDestroy(h->up[i]);
         cudaFree(h->d_in[i]);
@@ -159,7 +165,7 @@ TPRGB_API int tprgb_host_ctx_create(int64_t chunk_eq, tprgb_host_ctx **out) {
                     (long long)chunk_eq);
     tprgb_host_ctx *h = new tprgb_host_ctx();
     h->chunk_eq = chunk_eq;
-    for (int i = 0; i < 2; i++) {
+    for (int i = 0; i < kHostStreams; i++) {
         cudaError_t e = cudaStreamCreateWithFlags(&h->st[i], cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->up[i], cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaMalloc(&h->d_in[i], 4 * sizeof(float) * (size_t)chunk_eq);
@@ -175,7 +181,7 @@ TPRGB_API int tprgb_host_ctx_create(int64_t chunk_eq, tprgb_host_ctx **out) {
 
 TPRGB_API int tprgb_host_ctx_destroy(tprgb_host_ctx *h) {
     if (!h) return fail(TPRGB_EINVAL, "ctx is NULL");
-    for (int i = 0; i < 2; i++) cudaStreamSynchronize(h->st[i]);
+    for (int i = 0; i < kHostStreams; i++) cudaStreamSynchronize(h->st[i]);
     host_ctx_free(h);
     return TPRGB_OK;
 }
@@ -199,7 +205,7 @@ TPRGB_API int tprgb_batch_solve_host(tprgb_host_ctx *h, int nsys, int n,
                     (long long)h->chunk_eq, n);
     const size_t xs = o.x_f64 ? sizeof(double) : sizeof(float);
     int k = 0;
-    for (int64_t s0 = 0; s0 < nsys; s0 += per, k ^= 1) {
+    for (int64_t s0 = 0; s0 < nsys; s0 += per, k = (k + 1) % kHostStreams) {
         const int64_t ns = std::min<int64_t>(per, nsys - s0);
         const int64_t off = s0 * n, neq = ns * n;
         cudaStream_t st = h->st[k];
@@ -215,8 +221,7 @@ TPRGB_API int tprgb_batch_solve_host(tprgb_host_ctx *h, int nsys, int n,
         TPRGB_CUDA(cudaMemcpyAsync((char *)x + off * xs, h->d_x[k], xs * (size_t)neq,
                                    cudaMemcpyDeviceToHost, st));
     }
-    TPRGB_CUDA(cudaStreamSynchronize(h->st[0]));
-    TPRGB_CUDA(cudaStreamSynchronize(h->st[1]));
+    for (int i = 0; i < kHostStreams; i++) TPRGB_CUDA(cudaStreamSynchronize(h->st[i]));
     return TPRGB_OK;
 }
 
