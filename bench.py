@@ -107,14 +107,24 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
+PROFILE = os.path.join(ROOT, "profiles", "batch_sw_n1024_full.md")
+
+
 def profiled_traffic():
-    """DRAM bytes per launch of the batched kernel from the committed ncu
-    summary (profiles/), or None."""
-    p = os.path.join(ROOT, "profiles", "batch_uniform_n1024_traffic.json")
-    if os.path.exists(p):
-        with open(p) as f:
-            return json.load(f).get("dram_bytes_per_launch")
-    return None
+    """DRAM bytes (read + write) per launch of the batched kernel, from the
+    committed ncu summary of the same workload (profiles/), or None."""
+    if not os.path.exists(PROFILE):
+        return None
+    got = {}
+    unit = {"byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9}
+    for line in open(PROFILE):
+        for key in ("DRAM read", "DRAM write"):
+            if line.startswith(f"| {key} |"):
+                v, u = line.split("|")[2].split()
+                got[key] = float(v) * unit.get(u, 1.0)
+    if len(got) != 2:
+        return None
+    return got["DRAM read"] + got["DRAM write"]
 
 
 def cpu_reference_sample(port_or_ref, bt, nsys_sample, threads):

@@ -392,6 +392,18 @@ TPRGB_API int tprgb_server_run_load(tprgb_server *srv, int nreq,
                                     double *detail_us, double *elapsed_s,
                                     long long *systems_out);
 
+/* ---- comparison solver -------------------------------------------------
+ * cuSPARSE gtsv2_nopivot on one system from host arrays, as the reference's
+ * benchmark runs it next to its own solvers (src/reference_cusparse.cu:
+ * 166-205, selected by "cusparse" in src/pm.cpp:86): copies in, the solve,
+ * copy out.  prec TPRGB_F32 / TPRGB_F64 (arrays of that type); diag NULL
+ * means a unit diagonal (the 3-argument form).  *device_ms (may be NULL):
+ * the solve alone, timed with CUDA events (the reference's device timer).
+ * libcusparse is opened at run time; TPRGB_EUNSUPPORTED where it is absent. */
+TPRGB_API int tprgb_cusparse_gtsv(int prec, int n, const void *a,
+                                  const void *diag, const void *c,
+                                  const void *rhs, void *x, float *device_ms);
+
 /* ---- diagnostics ------------------------------------------------------- */
 /* Status word of the TMA-staged batched kernel: *code = TPRGB_ETIMEOUT if a
  * bounded wait gave up since the last reset (reset != 0 clears it). */

@@ -35,3 +35,36 @@ def test_pm_cli(cuda, tmp_path):
         assert vals.shape == (1024,)
     times, x = pm.run(1024, 128, 64, "batch")
     assert len(times) == 64
+    times, x = pm.run(1024, 128, 3, "cusparse", str(out))
+    assert len(times) == 3 and np.isfinite(x).all() and min(times) > 0
+
+
+def test_cusparse_comparator(cuda, port, ans1024):
+    """The cuSPARSE gtsv2_nopivot comparison solver (the reference's
+    "cusparse" benchmark option) on the reference's fixed N=1024 system and
+    a random dominant one."""
+    import ctypes
+    import tpr_gb300 as T
+    from tpr_gb300 import generate as G
+    L = T.load()
+    n = 1024
+    a, diag, c, rhs = (v.astype(np.float32) for v in G.fixed_system(n))
+    x = np.empty(n, np.float32)
+    ms = ctypes.c_float()
+    ptr = lambda v: v.ctypes.data_as(ctypes.c_void_p)
+    T.check(L.tprgb_cusparse_gtsv(T.F32, n, ptr(a), None, ptr(c), ptr(rhs),
+                                  ptr(x), ctypes.byref(ms)))
+    ans = ans1024
+    # the reference's known-answer tolerances (test/examples.cpp:36-56)
+    assert np.all(np.abs(x - ans) <= 1e-2)
+    assert np.max((x - ans) ** 2) <= 1e-3
+    assert ms.value > 0
+    bt = G.batch(np.array([4096]), 3, "dominant")
+    for prec, dt, tol in ((T.F32, np.float32, 1e-5), (T.F64, np.float64, 1e-12)):
+        av, bv, cv, dv = (v.astype(dt) for v in (bt.a, bt.b, bt.c, bt.d))
+        xv = np.empty(4096, dt)
+        T.check(L.tprgb_cusparse_gtsv(prec, 4096, ptr(av), ptr(bv), ptr(cv),
+                                      ptr(dv), ptr(xv), None))
+        worst, _ = port.batch_rel_l2(bt, xv.astype(np.float64),
+                                     port.batch_thomas(bt))
+        assert worst <= tol, (prec, worst)

@@ -39,6 +39,7 @@ SOURCES = {
     "plan_kernels.cu": [],
     "gen_kernels.cu": [],
     "server.cu": [],
+    "cusparse_cmp.cu": [],
 }
 
 
@@ -97,7 +98,7 @@ def build(force: bool = False, verbose: bool = False, jobs: int = 0) -> str:
     if todo or not os.path.exists(LIB):
         tmp = LIB + ".tmp"
         cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + \
-              ["-lcudart", "-lpthread"]
+              ["-lcudart", "-lpthread", "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stderr}")

@@ -5,7 +5,9 @@
 SOLVER: tpr | ptpr | pcr | cr (reference-semantics GPU solvers through the
 class surface, timed per solve with the host round trip included, as the
 reference's CPU timers include get_ans), cutpr | cuptpr (the *_cu free
-functions, host arrays in and out), batch (ITER systems in one launch of
+functions, host arrays in and out), cusparse (cuSPARSE gtsv2_nopivot,
+device time of the solve as the reference's device timer measures it,
+src/reference_cusparse.cu:166-205), batch (ITER systems in one launch of
 the batched solver, FP32 + one refinement step).
 
 Input per iteration: a = c = -1/6, diag = 1, rhs ~ U(-1, 1) (the
@@ -23,7 +25,7 @@ import numpy as np
 
 import tpr_gb300 as T
 
-SOLVERS = ("tpr", "ptpr", "pcr", "cr", "cutpr", "cuptpr", "batch")
+SOLVERS = ("tpr", "ptpr", "pcr", "cr", "cutpr", "cuptpr", "cusparse", "batch")
 
 
 def _input(n, rng):
@@ -42,7 +44,18 @@ def run(n: int, s: int, iters: int, solver: str, out=None, seed: int = 0):
         raise SystemExit(f"Solver Not Found: {solver}")
     rng = np.random.default_rng(seed)
     times, x = [], None
-    if solver == "batch":
+    if solver == "cusparse":
+        import ctypes
+        L = T.load()
+        for _ in range(iters):
+            a, diag, c, rhs = _input(n, rng)
+            x = np.empty(n, np.float32)
+            ms = ctypes.c_float()
+            ptr = lambda v: v.ctypes.data_as(ctypes.c_void_p)
+            T.check(L.tprgb_cusparse_gtsv(T.F32, n, ptr(a), ptr(diag), ptr(c),
+                                          ptr(rhs), ptr(x), ctypes.byref(ms)))
+            times.append(ms.value)
+    elif solver == "batch":
         from . import batch as B
         from . import generate as G
         bt = G.batch(np.full(iters, n), seed, "dominant")
