@@ -16,7 +16,7 @@ from tpr_gb300 import nstab, pm
 def test_tune_table_apply_and_get(lib, tmp_path):
     from tpr_gb300 import batch as B
     lib.tprgb_tune_clear()
-    assert B.tile_for(1024)[:2] == (8, 256)          # built-in default
+    assert B.tile_for(1024) == (16, 64, 4)           # built-in default
     doc = {"device": "TEST-GPU", "tiles": {
         "1024": {"eq_per_thread": 4, "threads_per_cta": 512, "variant": 2},
         "64": {"eq_per_thread": 8, "threads_per_cta": 128, "variant": 1}}}
@@ -27,7 +27,7 @@ def test_tune_table_apply_and_get(lib, tmp_path):
     assert B.tile_for(1024) == (4, 512, 2)
     assert B.tile_for(64) == (8, 128, 1)
     lib.tprgb_tune_clear()
-    assert B.tile_for(1024)[:2] == (8, 256)
+    assert B.tile_for(1024) == (16, 64, 4)
 
 
 def test_tune_set_rejects_bad_tiles(lib):

@@ -5,14 +5,17 @@
 
 namespace tprgb {
 
-// Default tile per system size (equations per thread, threads per CTA),
+// Default tile per system size (equations per thread, threads per CTA,
+// variant): the tiles the autotuner measured fastest on GB300, so the
+// staged and cluster kernels serve calls even without a loaded table;
 // replaced at run time by the autotuner's table when one is loaded.
 TileConfig default_tile(int n) {
-    if (n <= 64) return TileConfig{4, 256};
-    if (n <= 1024) return TileConfig{8, 256};
-    if (n <= 2048) return TileConfig{8, 256};
-    if (n <= 4096) return TileConfig{8, 512};
-    if (n <= 8192) return TileConfig{8, 1024};
+    if (n < 32) return TileConfig{8, 128, 1};     // bulk-copy staged ring
+    if (n <= 256) return TileConfig{8, 64, 2};    // swizzled, two stages
+    if (n <= 1024) return TileConfig{16, 64, 3};  // swizzled, one stage
+    if (n <= 2048) return TileConfig{16, 128, 3};
+    if (n <= 4096) return TileConfig{16, 128, 4};  // clusters of 2
+    if (n <= 16384) return TileConfig{16, n <= 8192 ? 256 : 128, 4};
     return TileConfig{16, 256, 4};  // one cluster of n / 4096 CTAs per system
 }
 
@@ -107,23 +110,25 @@ TPRGB_API int tprgb_batch_solve(int nsys, int n, const float *d_a,
     const bool staged_ok = (cfg.nt == 128 || cfg.nt == 256 || cfg.nt == 512) && !f64_resid;
     const bool sw_ok = (cfg.nt == 64 || cfg.nt == 128 || cfg.nt == 256) && n >= 32 &&
                        (cfg.L == 8 || cfg.L == 16) && !f64_resid;
-    if (cfg.staged == 4) {
-        if (f64_resid)
-            return fail(TPRGB_EUNSUPPORTED, "systems of %d equations need the cluster "
-                                            "kernel, which has no FP64 residual mode", n);
-        return launch_batch_cl(A, cfg, (cudaStream_t)stream);
-    }
-    if (cfg.staged >= 2 && sw_ok) return launch_batch_sw(A, cfg, (cudaStream_t)stream);
-    if (cfg.staged == 1 && staged_ok)
+    int P = 0;
+    const bool cl_ok = cfg.staged == 4 && !f64_resid && cfg.L == 16 &&
+                       (cfg.nt == 64 || cfg.nt == 128 || cfg.nt == 256) &&
+                       n % (16 * cfg.nt) == 0 && (P = n / (16 * cfg.nt)) >= 2 && P <= 16;
+    if (cl_ok) return launch_batch_cl(A, cfg, (cudaStream_t)stream);
+    if (cfg.staged == 2 || cfg.staged == 3) {
+        if (sw_ok) return launch_batch_sw(A, cfg, (cudaStream_t)stream);
+    } else if (cfg.staged == 1 && staged_ok) {
         return launch_batch_tma(A, cfg, (cudaStream_t)stream);
+    }
     if (o.variant >= 2)
         return fail(TPRGB_EUNSUPPORTED,
-                    "variant %d does not serve this tile (threads %d, n %d) or residual",
-                    o.variant, cfg.nt, n);
-    // a tuned staged tile that cannot serve this call (FP64 residual): the
-    // register kernel with the same shape where that is valid
-    if (cfg.L == 16) cfg.L = 8;
-    if (cfg.nt < 128) cfg.nt = 128;
+                    "variant %d does not serve this tile (L %d, threads %d, n %d) or residual",
+                    o.variant, cfg.L, cfg.nt, n);
+    // The table's kernel cannot serve this call (a caller-chosen shape, or
+    // the FP64 residual, which only the register kernel has): the register
+    // kernel, with the caller's shape where given, else one that covers n.
+    if (!o.eq_per_thread) cfg.L = n >= 16 ? 8 : 4;
+    if (!o.threads_per_cta) cfg.nt = std::min(1024, std::max(128, n / cfg.L));
     cfg.staged = 0;
     return launch_batch_uniform(A, cfg, (cudaStream_t)stream);
 }
