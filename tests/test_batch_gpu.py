@@ -1,6 +1,8 @@
 """Batched hierarchical solver against the FP64 Thomas oracle (FP32-stored
 systems).  Tolerances: plain FP32 solve <= 1e-5 relative L2 per system;
 with refinement <= 1e-9 (the accuracy target of the refined solver)."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -207,3 +209,27 @@ def test_cluster_default_and_rejects(cuda, port):
                      eq_per_thread=16, threads_per_cta=64, variant=B.CLUSTER)
     with pytest.raises(T.TprError):   # FP64 residual
         B.solve_host(bt, refine_steps=1, residual=B.RESID_F64)
+
+
+@pytest.mark.parametrize("n,nsys,L,nt,v", [
+    (32, 1, 8, 64, B.SWIZZLED),        # smallest swizzled size, one system
+    (1024, 1, 16, 64, B.SWIZZLED_ONE),  # one system, one CTA
+    (512, 3, 16, 256, B.SWIZZLED),      # fewer systems than one tile holds
+    (4096, 1, 16, 128, B.CLUSTER),      # one system, one cluster of 2
+    (65536, 1, 16, 256, B.CLUSTER),     # one system, one cluster of 16
+])
+def test_small_batches_edge_tiles(cuda, port, n, nsys, L, nt, v):
+    bt = G.uniform_batch(nsys, n, 300 + n + nsys, "uneven")
+    x = B.solve_host(bt, refine_steps=1, eq_per_thread=L, threads_per_cta=nt,
+                     variant=v)
+    worst, _ = _err(port, bt, x)
+    assert worst <= 1e-9, worst
+
+
+@pytest.mark.parametrize("v,n,L,nt", [(B.SWIZZLED, 1024, 16, 64),
+                                     (B.CLUSTER, 4096, 16, 128), (0, 4096, 0, 0)])
+def test_empty_batch_is_a_no_op(cuda, v, n, L, nt):
+    o = B.opts(refine_steps=1, eq_per_thread=L, threads_per_cta=nt, variant=v)
+    rc = B.load().tprgb_batch_solve(0, n, None, None, None, None, None,
+                                    ctypes.byref(o), None)
+    assert rc == 0
