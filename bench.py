@@ -246,7 +246,7 @@ def run_ours(args):
         pin = [torch.from_numpy(v).pin_memory() for v in
                (bt.a, bt.b, bt.c, bt.d)]
         xh = torch.empty(NSYS * N, dtype=torch.float64).pin_memory()
-        ctx = B.HostContext(chunk_eq=1 << 21)
+        ctx = B.HostContext(chunk_eq=1 << 22)
         for _ in range(2):
             ctx.solve(NSYS, N, *pin, xh, o)
         torch.cuda.synchronize()

@@ -233,3 +233,21 @@ def test_empty_batch_is_a_no_op(cuda, v, n, L, nt):
     rc = B.load().tprgb_batch_solve(0, n, None, None, None, None, None,
                                     ctypes.byref(o), None)
     assert rc == 0
+
+
+@pytest.mark.parametrize("nsys,chunk_systems", [(300, 32), (40, 32), (7, 64)])
+def test_host_pipeline_matches_device_solve(cuda, nsys, chunk_systems):
+    """tprgb_batch_solve_host (host arrays, chunks ramped 1/8, 1/4, 1/2 of a
+    full chunk at both ends over three streams; small batches in equal
+    chunks) gives the same bits as the device-resident solve."""
+    import torch
+    n = 1024
+    bt = G.uniform_batch(nsys, n, 4242 + nsys, "uneven")
+    want = B.solve_host(bt, refine_steps=1)
+    pin = [torch.from_numpy(v).pin_memory() for v in (bt.a, bt.b, bt.c, bt.d)]
+    x = torch.zeros(nsys * n, dtype=torch.float64).pin_memory()
+    ctx = B.HostContext(chunk_eq=chunk_systems * n)
+    for _ in range(2):   # repeated calls reuse the context
+        x.zero_()
+        ctx.solve(nsys, n, *pin, x, B.opts(refine_steps=1))
+        np.testing.assert_array_equal(x.numpy(), want)

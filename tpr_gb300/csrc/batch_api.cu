@@ -1,5 +1,6 @@
 // C ABI of the batched solver: options, tile selection, uniform batches.
 #include <algorithm>
+#include <vector>
 
 #include "batch.cuh"
 
@@ -209,9 +210,33 @@ TPRGB_API int tprgb_batch_solve_host(tprgb_host_ctx *h, int nsys, int n,
         return fail(TPRGB_EINVAL, "chunk of %lld equations < one system (n=%d)",
                     (long long)h->chunk_eq, n);
     const size_t xs = o.x_f64 ? sizeof(double) : sizeof(float);
+    // Chunk sizes ramp up (1/8, 1/4, 1/2 of a full chunk) at the start and
+    // down again at the end: the first solve and the first download start
+    // sooner and the last chunk's solve and download are short, so less of
+    // the link time is spent filling and draining the pipeline.
+    std::vector<int64_t> sizes;
+    {
+        const int64_t ramp[3] = {std::max<int64_t>(1, per >> 3),
+                                 std::max<int64_t>(1, per >> 2),
+                                 std::max<int64_t>(1, per >> 1)};
+        const int64_t edges = 2 * (ramp[0] + ramp[1] + ramp[2]);
+        if (nsys > edges + per) {
+            for (int64_t v : ramp) sizes.push_back(v);
+            int64_t mid = nsys - edges;
+            while (mid > 0) {
+                sizes.push_back(std::min(per, mid));
+                mid -= per;
+            }
+            for (int i = 2; i >= 0; i--) sizes.push_back(ramp[i]);
+        } else {
+            for (int64_t s0 = 0; s0 < nsys; s0 += per)
+                sizes.push_back(std::min<int64_t>(per, nsys - s0));
+        }
+    }
     int k = 0;
-    for (int64_t s0 = 0; s0 < nsys; s0 += per, k = (k + 1) % kHostStreams) {
-        const int64_t ns = std::min<int64_t>(per, nsys - s0);
+    int64_t s0 = 0;
+    for (size_t ci = 0; ci < sizes.size(); ci++, k = (k + 1) % kHostStreams) {
+        const int64_t ns = sizes[ci];
         const int64_t off = s0 * n, neq = ns * n;
         cudaStream_t st = h->st[k];
         float *da = h->d_in[k], *db = da + h->chunk_eq, *dc = db + h->chunk_eq,
@@ -225,6 +250,7 @@ TPRGB_API int tprgb_batch_solve_host(tprgb_host_ctx *h, int nsys, int n,
         if (rc) return rc;
         TPRGB_CUDA(cudaMemcpyAsync((char *)x + off * xs, h->d_x[k], xs * (size_t)neq,
                                    cudaMemcpyDeviceToHost, st));
+        s0 += ns;
     }
     for (int i = 0; i < kHostStreams; i++) TPRGB_CUDA(cudaStreamSynchronize(h->st[i]));
     return TPRGB_OK;
