@@ -156,10 +156,11 @@ struct Plan {
     cudaGraphExec_t gexec = nullptr;
     const void *g_ptrs[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     cudaStream_t cap_stream = nullptr;
-    // cluster and staged routes run on two side streams forked from the
+    // routed size groups run on kPlanSides side streams forked from the
     // caller's stream (joined before the queue kernel)
-    cudaStream_t side[2] = {nullptr, nullptr};
-    cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
+    static constexpr int kPlanSides = 3;
+    cudaStream_t side[kPlanSides] = {};
+    cudaEvent_t fork = nullptr, join[kPlanSides] = {};
 };
 
 TileConfig tuned_tile(int n);  // batch_api.cu
@@ -307,7 +308,7 @@ static void plan_free(Plan *p) {
     if (!p) return;
     if (p->gexec) cudaGraphExecDestroy(p->gexec);
     if (p->cap_stream) cudaStreamDestroy(p->cap_stream);
-    for (int i = 0; i < 2; i++) {
+    for (int i = 0; i < Plan::kPlanSides; i++) {
         if (p->side[i]) cudaStreamDestroy(p->side[i]);
         if (p->join[i]) cudaEventDestroy(p->join[i]);
     }
@@ -406,21 +407,21 @@ static int plan_reset(Plan *p, cudaStream_t st) {
     return TPRGB_OK;
 }
 
-// One launch per routed size group (largest first): the cluster groups on
-// one side stream, the staged groups on another, so that one kernel's
-// tail overlaps the next group; then, after both join the caller's
-// stream, the queue kernel for the remaining systems (its multi-CTA
-// barriers assume all of its CTAs become resident, so it runs alone).
+// One launch per routed size group, largest first, dealt round-robin onto
+// the side streams, so that groups of different sizes (cluster sizes that
+// leave SMs idle, staged groups, the kernels' tails) run side by side;
+// then, after the side streams join the caller's stream, the queue kernel
+// for the remaining systems (its multi-CTA barriers assume all of its CTAs
+// become resident, so it runs alone).
 static int plan_launch(Plan *p, const float *a, const float *b, const float *c,
                        const float *d, void *x, cudaStream_t st) {
     int rc = plan_reset(p, st);
     if (rc) return rc;
     unsigned *sys_status = p->d_ctl + 16 + p->nlarge;
-    bool kinds[3] = {false, false, false};
-    for (const Route &r : p->routes) kinds[r.kind] = true;
-    const bool fork = kinds[1] && kinds[2];
+    const int nsides = std::min<int>(Plan::kPlanSides, (int)p->routes.size());
+    const bool fork = nsides > 1;
     if (fork) {
-        for (int i = 0; i < 2; i++) {
+        for (int i = 0; i < nsides; i++) {
             if (!p->side[i])
                 TPRGB_CUDA(cudaStreamCreateWithFlags(&p->side[i], cudaStreamNonBlocking));
             if (!p->join[i])
@@ -428,20 +429,22 @@ static int plan_launch(Plan *p, const float *a, const float *b, const float *c,
         }
         if (!p->fork) TPRGB_CUDA(cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming));
         TPRGB_CUDA(cudaEventRecord(p->fork, st));
-        for (int i = 0; i < 2; i++) TPRGB_CUDA(cudaStreamWaitEvent(p->side[i], p->fork, 0));
+        for (int i = 0; i < nsides; i++)
+            TPRGB_CUDA(cudaStreamWaitEvent(p->side[i], p->fork, 0));
     }
+    int ri = 0;
     for (const Route &r : p->routes) {
         BatchArgs A{a, b, c, d, x, r.count, r.n, p->refine_steps, p->residual, p->x_f64};
         A.sys_off = p->d_off + r.first;
         A.sys_status = sys_status + r.first;
         A.status = p->d_ctl + 4;
         A.total_eq = p->total_eq;
-        cudaStream_t rs = fork ? p->side[r.kind == 2 ? 0 : 1] : st;
+        cudaStream_t rs = fork ? p->side[ri++ % nsides] : st;
         rc = r.kind == 2 ? launch_batch_cl(A, r.cfg, rs) : launch_batch_sw(A, r.cfg, rs);
         if (rc) return rc;
     }
     if (fork) {
-        for (int i = 0; i < 2; i++) {
+        for (int i = 0; i < nsides; i++) {
             TPRGB_CUDA(cudaEventRecord(p->join[i], p->side[i]));
             TPRGB_CUDA(cudaStreamWaitEvent(st, p->join[i], 0));
         }

@@ -142,10 +142,11 @@ struct Server {
     RangeAlloc *alloc = nullptr;
     cudaStream_t prep = nullptr, comp = nullptr;
     cudaEvent_t prep_ev[2] = {nullptr, nullptr};
-    // a step's cluster and staged size groups run on two side streams
-    // forked from comp and joined before its queue kernel
-    cudaStream_t side[2] = {nullptr, nullptr};
-    cudaEvent_t fork_ev = nullptr, join_ev[2] = {nullptr, nullptr};
+    // a step's routed size groups run on kSides side streams forked from
+    // comp and joined before its queue kernel
+    static constexpr int kSides = 3;
+    cudaStream_t side[kSides] = {};
+    cudaEvent_t fork_ev = nullptr, join_ev[kSides] = {};
     // per step buffers (double-buffered): items, offsets, ctl, scratch,
     // generator tables
     struct Buf {
@@ -361,16 +362,17 @@ static int launch_step(Server *s) {
                                cudaMemcpyHostToDevice, cs));
     TPRGB_CUDA(cudaMemcpyAsync(b.ctl, b.h_ctl, sizeof(unsigned) * ctl_words,
                                cudaMemcpyHostToDevice, cs));
-    // size groups on the staged / cluster kernels (largest first; the two
-    // kinds on two side streams), the rest on the queue kernel after both
-    // join
-    bool kinds[3] = {false, false, false};
-    for (const Route &r : routes) kinds[r.kind] = true;
-    const bool fork = kinds[1] && kinds[2];
+    // size groups on the staged / cluster kernels (largest first, dealt
+    // round-robin onto the side streams), the rest on the queue kernel
+    // after the side streams join
+    const int nsides = std::min<int>(Server::kSides, (int)routes.size());
+    const bool fork = nsides > 1;
     if (fork) {
         TPRGB_CUDA(cudaEventRecord(s->fork_ev, cs));
-        for (int i = 0; i < 2; i++) TPRGB_CUDA(cudaStreamWaitEvent(s->side[i], s->fork_ev, 0));
+        for (int i = 0; i < nsides; i++)
+            TPRGB_CUDA(cudaStreamWaitEvent(s->side[i], s->fork_ev, 0));
     }
+    int ri = 0;
     for (const Route &r : routes) {
         BatchArgs A{s->A, s->B, s->Cc, s->D, s->X, r.count, r.n, s->o.refine_steps,
                     s->o.residual, 1};
@@ -378,12 +380,12 @@ static int launch_step(Server *s) {
         A.sys_status = b.ctl + 16 + nlarge + r.first;
         A.status = b.ctl + 4;
         A.total_eq = s->cap_eq;
-        cudaStream_t rs = fork ? s->side[r.kind == 2 ? 0 : 1] : cs;
+        cudaStream_t rs = fork ? s->side[ri++ % nsides] : cs;
         rc = r.kind == 2 ? launch_batch_cl(A, r.cfg, rs) : launch_batch_sw(A, r.cfg, rs);
         if (rc) return rc;
     }
     if (fork) {
-        for (int i = 0; i < 2; i++) {
+        for (int i = 0; i < nsides; i++) {
             TPRGB_CUDA(cudaEventRecord(s->join_ev[i], s->side[i]));
             TPRGB_CUDA(cudaStreamWaitEvent(cs, s->join_ev[i], 0));
         }
@@ -519,7 +521,7 @@ static void server_free(Server *s) {
     }
     if (s->comp) cudaStreamSynchronize(s->comp);
     if (s->prep) cudaStreamSynchronize(s->prep);
-    for (int i = 0; i < 2; i++) {
+    for (int i = 0; i < Server::kSides; i++) {
         if (s->side[i]) {
             cudaStreamSynchronize(s->side[i]);
             cudaStreamDestroy(s->side[i]);
@@ -662,7 +664,7 @@ TPRGB_API int tprgb_server_create(const tprgb_server_opts *opts,
     }
     for (auto &e : s->step_ev)
         if (cudaEventCreateWithFlags(&e, cudaEventDefault) != cudaSuccess) rc = TPRGB_ECUDA;
-    for (int i = 0; i < 2; i++) {
+    for (int i = 0; i < Server::kSides; i++) {
         if (cudaStreamCreateWithFlags(&s->side[i], cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreateWithFlags(&s->join_ev[i], cudaEventDisableTiming) != cudaSuccess)
             rc = TPRGB_ECUDA;
