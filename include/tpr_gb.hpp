@@ -21,8 +21,10 @@
 // errors throw tprgb::Error instead of exit()/abort().
 #pragma once
 
+#include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "tpr_gb.h"
 
@@ -122,6 +124,135 @@ class PCR : public Solver<TPRGB_PCR> {
         (void)diag;
         set_tridiagonal_system(a, c, rhs);
     }
+};
+
+// ---- batched solving (no counterpart in the reference, whose benchmark
+// loops over single systems, src/pm.cpp:224-238): RAII wrappers over the C
+// ABI's batch, host-pipeline, plan and server entry points.  Every call
+// throws tprgb::Error on a non-OK status. -----------------------------------
+
+// tprgb_batch_opts with the library defaults (FP32 + 1 refinement step,
+// compensated residual, FP64 x, tuned tile).
+struct BatchOptions : tprgb_batch_opts {
+    BatchOptions() { check(tprgb_batch_opts_default(this)); }
+    BatchOptions &refine(int steps) {
+        refine_steps = steps;
+        return *this;
+    }
+    BatchOptions &fp32_output() {
+        x_f64 = 0;
+        return *this;
+    }
+};
+
+// nsys systems of n equations back to back in device arrays; asynchronous
+// on `stream` (a cudaStream_t, or nullptr for the default stream).
+inline void batch_solve(int nsys, int n, const float *d_a, const float *d_b,
+                        const float *d_c, const float *d_d, void *d_x,
+                        const BatchOptions &o = BatchOptions(),
+                        void *stream = nullptr) {
+    check(tprgb_batch_solve(nsys, n, d_a, d_b, d_c, d_d, d_x, &o, stream));
+}
+
+// Host arrays in and out (pinned for full link speed); device buffers for
+// chunks of up to chunk_eq equations are allocated once, here.
+class HostPipeline {
+   public:
+    explicit HostPipeline(int64_t chunk_eq = int64_t(1) << 22) {
+        check(tprgb_host_ctx_create(chunk_eq, &h_));
+    }
+    HostPipeline(const HostPipeline &) = delete;
+    HostPipeline &operator=(const HostPipeline &) = delete;
+    ~HostPipeline() {
+        if (h_) tprgb_host_ctx_destroy(h_);
+    }
+    // x: double[nsys * n] (float[] with o.fp32_output()); synchronous
+    void solve(int nsys, int n, const float *a, const float *b, const float *c,
+               const float *d, void *x, const BatchOptions &o = BatchOptions()) {
+        check(tprgb_batch_solve_host(h_, nsys, n, a, b, c, d, x, &o));
+    }
+
+   private:
+    tprgb_host_ctx *h_ = nullptr;
+};
+
+// Uneven batch: sizes and offsets fixed at construction, executed many
+// times (optionally replayed from a CUDA graph).
+class Plan {
+   public:
+    Plan(int nsys, const int64_t *offsets, const int *ns,
+         const BatchOptions &o = BatchOptions(), bool graph = true)
+        : nsys_(nsys) {
+        check(tprgb_plan_create(nsys, offsets, ns, &o, &p_));
+        check(tprgb_plan_use_graph(p_, graph ? 1 : 0));
+    }
+    Plan(const Plan &) = delete;
+    Plan &operator=(const Plan &) = delete;
+    ~Plan() {
+        if (p_) tprgb_plan_destroy(p_);
+    }
+    void execute(const float *d_a, const float *d_b, const float *d_c,
+                 const float *d_d, void *d_x, void *stream = nullptr) {
+        check(tprgb_plan_execute(p_, d_a, d_b, d_c, d_d, d_x, stream));
+    }
+    // Waits for `stream`; per-system flags (1: non-finite solution) in the
+    // caller's order.  Returns the status instead of throwing on
+    // TPRGB_ENONFINITE, the expected outcome for singular systems.
+    int status(std::vector<unsigned> &per_system, void *stream = nullptr) {
+        per_system.assign((size_t)nsys_, 0u);
+        unsigned code = 0;
+        const int rc = tprgb_plan_status(p_, per_system.data(), &code, stream);
+        if (rc != TPRGB_OK && rc != TPRGB_ENONFINITE) check(rc);
+        return rc;
+    }
+
+   private:
+    int nsys_;
+    tprgb_plan *p_ = nullptr;
+};
+
+// Continuous-batching server over a device arena.
+class Server {
+   public:
+    explicit Server(size_t budget_bytes = size_t(8) << 30) {
+        tprgb_server_opts o;
+        check(tprgb_server_opts_default(&o));
+        o.budget_bytes = budget_bytes;
+        check(tprgb_server_create(&o, &s_));
+    }
+    explicit Server(const tprgb_server_opts &o) { check(tprgb_server_create(&o, &s_)); }
+    Server(const Server &) = delete;
+    Server &operator=(const Server &) = delete;
+    ~Server() {
+        if (s_) tprgb_server_destroy(s_);
+    }
+    // Host request: a..d stay valid until the request is done; x (may be
+    // null) receives the FP64 solution.
+    uint64_t submit(int nsys, const int *ns, const float *a, const float *b,
+                    const float *c, const float *d, double *x) {
+        uint64_t t = 0;
+        check(tprgb_server_submit_host(s_, nsys, ns, a, b, c, d, x, &t));
+        return t;
+    }
+    uint64_t submit_seeded(int nsys, const int *ns, const uint64_t *seeds,
+                           int kind = 1 /* uneven */) {
+        uint64_t t = 0;
+        check(tprgb_server_submit_seeded(s_, nsys, ns, seeds, kind, &t));
+        return t;
+    }
+    // Waits for the request; returns its status (TPRGB_ENONFINITE for a
+    // request with a non-finite system) and fills info.
+    int wait(uint64_t ticket, tprgb_request_info *info = nullptr, int timeout_ms = -1) {
+        tprgb_request_info local;
+        const int rc = tprgb_server_wait(s_, ticket, timeout_ms, info ? info : &local);
+        if (rc != TPRGB_OK && rc != TPRGB_ENONFINITE) check(rc);
+        return rc;
+    }
+    void fetch(uint64_t ticket, double *x_host) { check(tprgb_server_fetch(s_, ticket, x_host)); }
+    void release(uint64_t ticket) { check(tprgb_server_release(s_, ticket)); }
+
+   private:
+    tprgb_server *s_ = nullptr;
 };
 
 }  // namespace tprgb

@@ -108,8 +108,9 @@ def test_non_finite_system_is_flagged(cuda):
 
 
 def test_routes_by_size(cuda, port):
-    """Sizes 2^6..2^16 back to back: 256..4096 on the staged kernel,
-    8192..65536 on the cluster kernel, 64 and 128 on the queue kernel; one
+    """Sizes 2^6..2^16 back to back: sizes whose tile is a cluster tile
+    (and all of 8192..65536) on the cluster kernel, the other sizes of
+    256..4096 on the staged kernel, 64 and 128 on the queue kernel; one
     launch per routed size plus one queue launch; graph replay gives the
     same bits."""
     ns = G.uneven_sizes(120, 6, 16, 17)
@@ -117,8 +118,10 @@ def test_routes_by_size(cuda, port):
     info = {}
     x, (rc, st, code) = B.solve_plan_host(bt, refine_steps=1, info=info)
     assert rc == 0 and code == 0 and not st.any()
-    staged = int(((ns >= 256) & (ns <= 4096)).sum())
-    clus = int((ns >= 8192).sum())
+    on_cluster = {n: n >= 8192 or (n >= 2048 and B.tile_for(n)[2] == B.CLUSTER)
+                  for n in set(int(v) for v in ns)}
+    clus = int(sum(on_cluster[int(n)] for n in ns))
+    staged = int(sum((256 <= n <= 4096) and not on_cluster[int(n)] for n in ns))
     assert info["staged_systems"] == staged
     assert info["cluster_systems"] == clus
     assert info["queue_systems"] == len(ns) - staged - clus

@@ -183,13 +183,20 @@ static const void *plan_kernel(int nt, int mode) {
 
 // Staged or cluster kernel for the sorted systems [k, e) of size n, if one
 // serves them: offsets multiples of 32 equations (rows of the tensor-map
-// loads), 256 <= n <= 4096 (one CTA per system, swizzled staging) or
-// 8192 <= n <= 65536 (one thread-block cluster per system).
+// loads); the tile table's cluster tile where it names one, else
+// 256 <= n <= 4096 one CTA per system (swizzled staging) and
+// 8192 <= n <= 65536 one thread-block cluster per system.
 static bool route_for(int n, const std::vector<long long> &off, int k, int e,
                       Route &r) {
     for (int i = k; i < e; i++)
         if (off[i] & 31) return false;
     TileConfig c = tuned_tile(n);
+    // the table's cluster tile wherever it names one (n = 2048 ... 65536)
+    if (c.staged == 4 && c.L == 16 && (c.nt == 64 || c.nt == 128 || c.nt == 256) &&
+        n % (16 * c.nt) == 0 && n / (16 * c.nt) >= 2 && n / (16 * c.nt) <= 16) {
+        r = Route{2, n, k, e - k, c};
+        return true;
+    }
     if (n >= 256 && n <= 4096) {
         const bool sw = (c.staged == 2 || c.staged == 3) && (c.L == 8 || c.L == 16) &&
                         (c.nt == 64 || c.nt == 128 || c.nt == 256) && n / c.L <= c.nt;
