@@ -36,7 +36,7 @@ CANDIDATES = [(4, 128, 1), (4, 256, 1), (4, 512, 1), (4, 1024, 1),
               (8, 128, 2), (8, 256, 2), (8, 512, 2),
               (8, 64, 3), (8, 128, 3), (8, 256, 3),
               (16, 64, 3), (16, 128, 3), (16, 256, 3),
-              (8, 128, 4), (16, 64, 4), (16, 128, 4),
+              (8, 128, 4), (16, 64, 4), (16, 128, 4), (16, 256, 4),
               (16, 64, 5), (16, 128, 5), (16, 256, 5)]
 VARIANT_TAG = {1: "", 2: "s", 3: "w", 4: "w1", 5: "c"}
 

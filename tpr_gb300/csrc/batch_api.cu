@@ -15,7 +15,7 @@ TileConfig default_tile(int n) {
     if (n <= 256) return TileConfig{8, 64, 2};    // swizzled, two stages
     if (n <= 1024) return TileConfig{16, 64, 3};  // swizzled, one stage
     if (n <= 2048) return TileConfig{16, 128, 3};
-    if (n <= 4096) return TileConfig{16, 128, 4};  // clusters of 2
+    if (n <= 4096) return TileConfig{16, 256, 3};
     if (n <= 16384) return TileConfig{16, n <= 8192 ? 256 : 128, 4};
     return TileConfig{16, 256, 4};  // one cluster of n / 4096 CTAs per system
 }
