@@ -228,14 +228,18 @@ batch_cl(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
         pc.round = round;
         pc.nsolve = 0;
         const long long base = sys_base(sys) + (long long)p * TILE + tid * L;
+        // the next system's part starts loading as soon as this one's last
+        // read of the stage is done, overlapping the rest of the solve
+        auto early = [&]() {
+            __syncthreads();  // every thread is done reading the stage
+            if (tid == 0 && !pending && sys + nclusters < nsys) issue(sys + nclusters);
+        };
         const bool finite = tile::run_tile_smem<L, NT, NT, MODE, true>(
             stage, stage + TILE, stage + 2 * TILE, stage + 3 * TILE, off, gx,
             ok ? base : 0, ok, tid, p == 0 && tid == 0,
-            p == P - 1 && tid == NT - 1, refine_steps, x_f64, sm, pc);
+            p == P - 1 && tid == NT - 1, refine_steps, x_f64, sm, pc, early);
         if (sys_status && ok && !finite) atomicOr(&sys_status[sys], 1u);
         round = pc.round;
-        __syncthreads();  // every thread is done reading the stage
-        if (tid == 0 && !pending && sys + nclusters < nsys) issue(sys + nclusters);
     }
     // no CTA leaves while another may still read its shared memory
     cl::sync();

@@ -473,17 +473,25 @@ __device__ __forceinline__ void swizzled_offsets(int tid, unsigned (&off)[L / 4]
     for (int j = 0; j < L / 4; j++) off[j] = b0 ^ ((((unsigned)j) ^ r7) << 4);
 }
 
+// No-op stage-free hook (run_tile_smem's default).
+struct NoHook {
+    __device__ __forceinline__ void operator()() const {}
+};
+
 // Same computation as run_tile, but a, b, c, d are re-read from shared
 // memory each time they are needed instead of being held in registers
 // through the refinement.  SW = false: sa..sd point at this thread's
 // contiguous chunk; SW = true: sa..sd are the array regions' bases and off
-// holds the chunk's swizzled unit offsets.
-template <int L, int NT, int T, int MODE, bool SW = false>
+// holds the chunk's swizzled unit offsets.  stage_free() is called by every
+// thread right after the tile's last read of the staged arrays (before the
+// last solve's reduction), so a one-stage kernel can start loading its next
+// tile there; the hook synchronises the CTA itself.
+template <int L, int NT, int T, int MODE, bool SW = false, typename Hook = NoHook>
 __device__ __forceinline__ bool run_tile_smem(
     const float *sa, const float *sb, const float *sc, const float *sd,
     const unsigned (&off)[L / 4], void *__restrict__ gx, long long base,
     bool active, int t, bool first_eq, bool last_eq, int refine_steps,
-    int x_f64, Smem<NT> &sm, Part &pc) {
+    int x_f64, Smem<NT> &sm, Part &pc, Hook stage_free = Hook()) {
     auto load4 = [&](float (&a)[L], float (&b)[L], float (&c)[L],
                      float (&d)[L]) {
         if (active) {
@@ -510,10 +518,12 @@ __device__ __forceinline__ bool run_tile_smem(
         if (first_eq) a[0] = 0.f;
         if (last_eq) c[L - 1] = 0.f;
     };
+    const bool refine = MODE == 1 && refine_steps > 0;
     float xh[L];
     {
         float a[L], b[L], c[L], d[L];
         load4(a, b, c, d);
+        if (!refine) stage_free();
         solve<L, NT, T>(a, b, c, d, xh, sm, pc);
     }
     float xlo[L];
@@ -534,6 +544,7 @@ __device__ __forceinline__ bool run_tile_smem(
             {
                 float a[L], b[L], c[L], d[L];
                 load4(a, b, c, d);
+                if (step == refine_steps - 1) stage_free();
                 solve<L, NT, T>(a, b, c, r, dx, sm, pc);
             }
 #pragma unroll
