@@ -546,6 +546,20 @@ __global__ void normalize_kernel(long long neq, T *a, const T *diag, T *c,
 
 static const size_t kFusedSmemLimit = 200 * 1024;
 
+// Raise a kernel's dynamic shared-memory limit to `smem` unless an earlier
+// call on this device already raised it at least that far (the attribute
+// is per function and device; setting it is a host call that would
+// otherwise cost every launch).  set_to[dev]: the limit set so far.
+template <typename K>
+static int smem_attr(K k, size_t smem, size_t (&set_to)[16]) {
+    int dev = 0;
+    TPRGB_CUDA(cudaGetDevice(&dev));
+    if (dev >= 0 && dev < 16 && set_to[dev] >= smem) return TPRGB_OK;
+    TPRGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (dev >= 0 && dev < 16) set_to[dev] = smem;
+    return TPRGB_OK;
+}
+
 template <typename T>
 static bool ref_uses_fused(int kind, int n, int s) {
     if (kind == TPRGB_CR || kind == TPRGB_PCR)
@@ -606,8 +620,11 @@ static int launch_tpr_kind(int nsys, int n, int s, const T *a, const T *c,
         size_t smem = (size_t)refk::fused_elems(n, s) * sizeof(T);
         int threads = std::min(refk::kThreads, std::max(64, n));
         auto k = refk::fused_tpr<T, KIND>;
-        TPRGB_CUDA(cudaFuncSetAttribute(
-            k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        {
+            static size_t set_to[16] = {};
+            int rc = smem_attr(k, smem, set_to);
+            if (rc) return rc;
+        }
         k<<<nsys, threads, smem, st>>>(a, c, r, x, n, s, stride);
         TPRGB_CUDA(cudaGetLastError());
         return TPRGB_OK;
@@ -619,8 +636,11 @@ static int launch_tpr_kind(int nsys, int n, int s, const T *a, const T *c,
         size_t smem = 3ULL * s * sizeof(T);
         int threads = std::min(refk::kThreads, std::max(64, s));
         auto k = refk::sliced_stage1<T, KIND>;
-        TPRGB_CUDA(cudaFuncSetAttribute(
-            k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        {
+            static size_t set_to[16] = {};
+            int rc = smem_attr(k, smem, set_to);
+            if (rc) return rc;
+        }
         k<<<dim3(m, nsys), threads, smem, st>>>(a, c, r, work, n, s, stride);
         TPRGB_CUDA(cudaGetLastError());
     }
@@ -628,8 +648,11 @@ static int launch_tpr_kind(int nsys, int n, int s, const T *a, const T *c,
         size_t smem = 4ULL * m * sizeof(T);
         int threads = std::min(refk::kThreads, std::max(64, m));
         auto k = refk::sliced_stage2<T, KIND>;
-        TPRGB_CUDA(cudaFuncSetAttribute(
-            k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        {
+            static size_t set_to[16] = {};
+            int rc = smem_attr(k, smem, set_to);
+            if (rc) return rc;
+        }
         k<<<nsys, threads, smem, st>>>(work, x, n, s, stride);
         TPRGB_CUDA(cudaGetLastError());
     }
@@ -637,9 +660,11 @@ static int launch_tpr_kind(int nsys, int n, int s, const T *a, const T *c,
         size_t smem = KIND == TPRGB_TPR ? (4ULL * s + 2) * sizeof(T) : 0;
         int threads = std::min(refk::kThreads, std::max(64, s));
         auto k = refk::sliced_stage3<T, KIND>;
-        if (smem)
-            TPRGB_CUDA(cudaFuncSetAttribute(
-                k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        if (smem) {
+            static size_t set_to[16] = {};
+            int rc = smem_attr(k, smem, set_to);
+            if (rc) return rc;
+        }
         k<<<dim3(m, nsys), threads, smem, st>>>(a, c, r, work, x, n, s, stride);
         TPRGB_CUDA(cudaGetLastError());
     }
@@ -662,8 +687,9 @@ static int launch_ref_t(int kind, int nsys, int n, int s, const T *a,
             int threads = std::min(refk::kThreads, std::max(64, n));
             auto k = kind == TPRGB_CR ? refk::fused_crpcr<T, TPRGB_CR>
                                       : refk::fused_crpcr<T, TPRGB_PCR>;
-            TPRGB_CUDA(cudaFuncSetAttribute(
-                k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            static size_t set_cr[16] = {}, set_pcr[16] = {};
+            int rc = smem_attr(k, smem, kind == TPRGB_CR ? set_cr : set_pcr);
+            if (rc) return rc;
             k<<<nsys, threads, smem, st>>>(a, c, r, x, n, stride);
             TPRGB_CUDA(cudaGetLastError());
             return TPRGB_OK;
