@@ -188,8 +188,8 @@ typedef struct tprgb_batch_opts {
                             5: one system per thread-block cluster of
                                P = n / (16 * threads) CTAs, P in {2, 4, 8,
                                16}, rows exchanged in distributed shared
-                               memory (16 equations per thread, 64/128/256
-                               threads)                                    */
+                               memory (16 equations per thread,
+                               64/128/256/512 threads)                     */
 } tprgb_batch_opts;
 
 /* Defaults: 1 refinement step, compensated residual, FP64 x, tuned tile. */

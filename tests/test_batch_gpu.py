@@ -169,7 +169,8 @@ def test_swizzled_rejects_bad_tiles(cuda):
 @pytest.mark.parametrize("n,nt,nsys", [(2048, 64, 5), (4096, 128, 3),
                                        (8192, 64, 9), (16384, 256, 4),
                                        (16384, 64, 100), (32768, 256, 3),
-                                       (65536, 256, 40)])
+                                       (65536, 256, 40), (16384, 512, 7),
+                                       (65536, 512, 10)])
 def test_cluster_kernel(cuda, port, n, nt, nsys):
     """One system per thread-block cluster (P = n / (16 nt) CTAs, boundary
     rows exchanged in distributed shared memory): refined solutions meet

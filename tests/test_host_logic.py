@@ -43,6 +43,8 @@ def test_tune_set_rejects_bad_tiles(lib):
     assert lib.tprgb_tune_set(1024, 16, 64, 5) == T.EINVAL     # one CTA
     assert lib.tprgb_tune_set(32768, 8, 256, 5) == T.EINVAL    # cluster L
     assert lib.tprgb_tune_set(32768, 16, 256, 5) == T.OK
+    assert lib.tprgb_tune_set(65536, 16, 512, 5) == T.OK       # 8 CTAs of 512
+    assert lib.tprgb_tune_set(8192, 16, 512, 5) == T.EINVAL    # one CTA of 512
     assert lib.tprgb_tune_set(1024, 16, 64, 4) == T.OK
     lib.tprgb_tune_clear()
 

@@ -29,7 +29,8 @@ TABLE = os.path.join(PKG, "tuned_tiles.json")
 SIZES = [16, 32, 64, 128, 256, 512, 1024, 2048, 4096, 8192, 16384, 32768,
          65536]
 # (equations per thread, threads per CTA, variant: 1 registers, 2 staged,
-# 3 swizzled staged with two stages, 4 swizzled with one stage)
+# 3 swizzled staged with two stages, 4 swizzled with one stage, 5 one
+# system per thread-block cluster)
 CANDIDATES = [(4, 128, 1), (4, 256, 1), (4, 512, 1), (4, 1024, 1),
               (8, 128, 1), (8, 256, 1), (8, 512, 1), (8, 1024, 1),
               (4, 128, 2), (4, 256, 2), (4, 512, 2),
@@ -38,6 +39,12 @@ CANDIDATES = [(4, 128, 1), (4, 256, 1), (4, 512, 1), (4, 1024, 1),
               (16, 64, 3), (16, 128, 3), (16, 256, 3),
               (8, 128, 4), (16, 64, 4), (16, 128, 4), (16, 256, 4),
               (16, 64, 5), (16, 128, 5), (16, 256, 5)]
+# Cluster CTAs of 512 threads (one per SM: 132 KB of staging) serve
+# n = 16384 .. 65536 when asked for explicitly.  Alone they time 5 % faster
+# than 256 threads at n = 65536 (0.213 vs 0.225 ms per 16.8 M equations), but
+# in a mixed-size plan, whose size groups run side by side, they took the
+# 4096-system uneven batch from 7.85 M to 6.85 M systems/s, so the uniform
+# timings here would mislead the table and they are not candidates.
 VARIANT_TAG = {1: "", 2: "s", 3: "w", 4: "w1", 5: "c"}
 
 

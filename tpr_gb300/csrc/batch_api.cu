@@ -53,9 +53,10 @@ TPRGB_API int tprgb_tune_set(int n, int eq_per_thread, int threads_per_cta,
     TileConfig c{eq_per_thread, threads_per_cta, variant >= 2 ? variant - 1 : 0};
     if (c.staged == 1 && c.nt != 128 && c.nt != 256 && c.nt != 512)
         return fail(TPRGB_EINVAL, "staged tiles use 128, 256 or 512 threads");
-    if (c.staged >= 2 && ((c.nt != 64 && c.nt != 128 && c.nt != 256) || n < 32))
+    if ((c.staged == 2 || c.staged == 3) &&
+        ((c.nt != 64 && c.nt != 128 && c.nt != 256) || n < 32))
         return fail(TPRGB_EINVAL, "swizzled tiles use 64, 128 or 256 threads and n >= 32");
-    int rc = batch_config_check(n, c);
+    int rc = batch_config_check(n, c);  // cluster tiles: cluster_parts' rules
     if (rc) return rc;
     int k = ilog2(n);
     g_tuned[k] = c;
@@ -113,7 +114,7 @@ TPRGB_API int tprgb_batch_solve(int nsys, int n, const float *d_a,
                        (cfg.L == 8 || cfg.L == 16) && !f64_resid;
     int P = 0;
     const bool cl_ok = cfg.staged == 4 && !f64_resid && cfg.L == 16 &&
-                       (cfg.nt == 64 || cfg.nt == 128 || cfg.nt == 256) &&
+                       (cfg.nt == 64 || cfg.nt == 128 || cfg.nt == 256 || cfg.nt == 512) &&
                        n % (16 * cfg.nt) == 0 && (P = n / (16 * cfg.nt)) >= 2 && P <= 16;
     if (cl_ok) return launch_batch_cl(A, cfg, (cudaStream_t)stream);
     if (cfg.staged == 2 || cfg.staged == 3) {

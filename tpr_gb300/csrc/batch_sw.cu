@@ -428,7 +428,7 @@ static int launch_cl_mode(const BatchArgs &A, int P, cudaStream_t st) {
     return launch_cl_t<16, NT, 1>(A, P, st);
 }
 
-// Cluster batch: 16 equations per thread, nt in {64, 128, 256} threads per
+// Cluster batch: 16 equations per thread, nt in {64, 128, 256, 512} threads per
 // CTA, P = n / (16 nt) CTAs per system with P in {2, 4, 8, 16}.
 int launch_batch_cl(const BatchArgs &A, const TileConfig &cfg, cudaStream_t st) {
     if (A.residual == TPRGB_RESID_F64 && A.refine_steps > 0)
@@ -438,13 +438,14 @@ int launch_batch_cl(const BatchArgs &A, const TileConfig &cfg, cudaStream_t st) 
     if (rc) return rc;
     if (A.nsys == 0) return TPRGB_OK;
     if (cfg.nt == 64) return launch_cl_mode<64>(A, P, st);
+    if (cfg.nt == 512) return launch_cl_mode<512>(A, P, st);
     return cfg.nt == 128 ? launch_cl_mode<128>(A, P, st) : launch_cl_mode<256>(A, P, st);
 }
 
 int cluster_parts(int n, const TileConfig &cfg, int *P) {
-    if (cfg.L != 16 || (cfg.nt != 64 && cfg.nt != 128 && cfg.nt != 256))
+    if (cfg.L != 16 || (cfg.nt != 64 && cfg.nt != 128 && cfg.nt != 256 && cfg.nt != 512))
         return fail(TPRGB_EINVAL, "cluster tiles use 16 equations per thread and 64, "
-                                  "128 or 256 threads");
+                                  "128, 256 or 512 threads");
     if (!is_pow2(n) || n < 2 * 16 * cfg.nt || n > 16 * 16 * cfg.nt)
         return fail(TPRGB_EINVAL, "n=%d needs 2..16 CTAs of %d equations", n, 16 * cfg.nt);
     *P = n / (16 * cfg.nt);

@@ -192,8 +192,8 @@ static bool route_for(int n, const std::vector<long long> &off, int k, int e,
         if (off[i] & 31) return false;
     TileConfig c = tuned_tile(n);
     // the table's cluster tile wherever it names one (n = 2048 ... 65536)
-    if (c.staged == 4 && c.L == 16 && (c.nt == 64 || c.nt == 128 || c.nt == 256) &&
-        n % (16 * c.nt) == 0 && n / (16 * c.nt) >= 2 && n / (16 * c.nt) <= 16) {
+    if (c.staged == 4 && c.L == 16 &&
+        (c.nt == 64 || c.nt == 128 || c.nt == 256 || c.nt == 512) && n % (16 * c.nt) == 0 && n / (16 * c.nt) >= 2 && n / (16 * c.nt) <= 16) {
         r = Route{2, n, k, e - k, c};
         return true;
     }
