@@ -169,6 +169,7 @@ batch_cl(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
     float *stage = reinterpret_cast<float *>(dyn_sw + pad);  // [4][TILE]
     __shared__ __align__(8) uint64_t full;
     __shared__ tile::Smem<NT> sm;
+    __shared__ float4 crows[tile::kClusterRowSlots];
     __shared__ int s_ok;
     const int tid = threadIdx.x;
     const unsigned P = cl::size(), p = cl::rank();
@@ -223,6 +224,7 @@ batch_cl(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
         }
         tile::Part pc;
         pc.on = 2;
+        pc.crows = crows;
         pc.P = (int)P;
         pc.p = (int)p;
         pc.round = round;

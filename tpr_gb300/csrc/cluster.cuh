@@ -1,5 +1,5 @@
 // Thread-block cluster primitives (inline PTX, sm_90+; used on sm_103a):
-// rank queries, the cluster-wide barrier, and loads from another CTA's
+// rank queries, the cluster-wide barrier, and stores to another CTA's
 // shared memory (distributed shared memory).
 #pragma once
 
@@ -22,8 +22,8 @@ __device__ __forceinline__ unsigned size() {
 }
 
 // Every thread of every CTA of the cluster arrives (release) and waits
-// (acquire): shared-memory writes before it are visible to loads from any
-// CTA of the cluster after it.  All threads of the cluster must execute
+// (acquire): shared-memory writes before it, to this CTA's or another
+// CTA's shared memory, are visible to every CTA of the cluster after it.  All threads of the cluster must execute
 // the same sequence of these barriers.
 __device__ __forceinline__ void sync() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
@@ -37,13 +37,11 @@ __device__ __forceinline__ uint32_t map(const void *p, unsigned r) {
     return out;
 }
 
-__device__ __forceinline__ float4 ld4(uint32_t addr) {
-    float4 v;
-    asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
-                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
-                 : "r"(addr)
+__device__ __forceinline__ void st4(uint32_t addr, float4 v) {
+    asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};"
+                 :
+                 : "r"(addr), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
                  : "memory");
-    return v;
 }
 
 }  // namespace cl

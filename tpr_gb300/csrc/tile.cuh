@@ -28,16 +28,21 @@ struct Smem {
     float4 edge[2 * (NT / 32)];
     float2 part_nb;  // previous part's last / next part's first unknown
     int ok;
-    float4 crow[2][2];  // cluster parts: this CTA's two boundary rows per parity
 };
+
+// Cluster parts' boundary rows as every CTA of a cluster holds them:
+// [parity][part][row 0 / 1], (a, c, d, 0) per row.
+constexpr int kClusterRowSlots = 2 * 16 * 2;
 
 // Multi-CTA system context.  on = 1: the parts are CTAs of a persistent
 // grid meeting at counter barriers in global scratch (per system: counter,
 // then rows [2 parity][32 parts][8 floats] and edges [2 parity][32 parts][4
 // floats]); on = 2: the parts are the CTAs of one thread-block cluster,
-// exchanging rows through distributed shared memory at cluster barriers.
+// exchanging rows through distributed shared memory at cluster barriers
+// (crows: this CTA's kClusterRowSlots-entry row buffer).
 struct Part {
     int on, P, p;
+    float4 *crows;
     unsigned *counter;
     float *rows, *edges;
     unsigned round;
@@ -148,14 +153,30 @@ __device__ __forceinline__ void solve(const float (&a)[L], const float (&b)[L],
                 hier::seg_reduce_k<W>(S0, S1, q2);
             }
             // level 3: this CTA's two boundary rows -> scratch (global
-            // memory, or this CTA's shared memory for cluster parts),
-            // barrier, every part solves the 2P-row system redundantly
+            // memory, or slot p of every cluster CTA's row buffer), barrier,
+            // every part solves the 2P-row system redundantly
             const unsigned par = pc.round & 1u;
             if (pc.on == 2) {
-                if (warp == 0 && lane == 0)
-                    sm.crow[par][0] = make_float4(S0.a, S0.c, S0.d, 0.f);
-                if (warp == 0 && lane == W - 1)
-                    sm.crow[par][1] = make_float4(S1.a, S1.c, S1.d, 0.f);
+                // lane j stores the rows into CTA j's buffer: remote stores
+                // complete under the barrier, and the level-3 reads after it
+                // are local (a remote read there would put a distributed
+                // shared-memory round trip on every part's critical path).
+                // A parity's slots are rewritten two barriers later, after
+                // every CTA has read them.
+                if (warp == 0) {
+                    const float a0 = __shfl_sync(0xffffffffu, S0.a, 0);
+                    const float c0 = __shfl_sync(0xffffffffu, S0.c, 0);
+                    const float d0 = __shfl_sync(0xffffffffu, S0.d, 0);
+                    const float a1 = __shfl_sync(0xffffffffu, S1.a, W - 1);
+                    const float c1 = __shfl_sync(0xffffffffu, S1.c, W - 1);
+                    const float d1 = __shfl_sync(0xffffffffu, S1.d, W - 1);
+                    if (lane < pc.P) {
+                        const uint32_t dst =
+                            cl::map(pc.crows + (par * 16 + pc.p) * 2, (unsigned)lane);
+                        cl::st4(dst, make_float4(a0, c0, d0, 0.f));
+                        cl::st4(dst + 16u, make_float4(a1, c1, d1, 0.f));
+                    }
+                }
                 cl::sync();
                 pc.round++;
             } else {
@@ -177,9 +198,9 @@ __device__ __forceinline__ void solve(const float (&a)[L], const float (&b)[L],
                 if (lane < P) {
                     float4 v0, v1;
                     if (pc.on == 2) {
-                        const uint32_t ra = cl::map(&sm.crow[par][0], (unsigned)lane);
-                        v0 = cl::ld4(ra);
-                        v1 = cl::ld4(ra + 16u);
+                        const float4 *src = pc.crows + (par * 16 + lane) * 2;
+                        v0 = src[0];
+                        v1 = src[1];
                     } else {
                         const float4 *src = reinterpret_cast<const float4 *>(pc.rows + (par * 32 + lane) * 8);
                         v0 = __ldcg(src);
