@@ -138,28 +138,37 @@ TPRGB_API int tprgb_batch_solve(int nsys, int n, const float *d_a,
 }  // extern "C"
 
 // ---- host-buffer pipeline -------------------------------------------------
-// Chunks rotate over kHostStreams streams, each with its own device buffers:
-// a chunk's upload waits only for the download of the chunk kHostStreams
-// earlier, so the host-to-device link stays busy while the previous chunks
-// solve and download.
-constexpr int kHostStreams = 3;
+// Three streams by role: uploads, solves and downloads, with kHostBufs input
+// and output buffers in a ring.  A chunk's upload waits only until the
+// solve of the chunk kHostBufs earlier has read its input buffer, and its
+// solve until that chunk's download has emptied the output buffer, so the
+// link carries uploads back to back while downloads of earlier chunks run
+// the other way.  (One stream per buffer, upload -> solve -> download in
+// order, made each upload also wait for a download: 2 % slower end to end.)
+constexpr int kHostBufs = 3;
 
 struct tprgb_host_ctx {
     int64_t chunk_eq = 0;
-    cudaStream_t st[kHostStreams] = {};
-    cudaEvent_t up[kHostStreams] = {};
-    float *d_in[kHostStreams] = {};  // a, b, c, d of one chunk
-    void *d_x[kHostStreams] = {};    // x of one chunk (8 B / eq)
+    cudaStream_t up = nullptr, solve = nullptr, down = nullptr;
+    cudaEvent_t uploaded[kHostBufs] = {}, solved[kHostBufs] = {}, downloaded[kHostBufs] = {};
+    float *d_in[kHostBufs] = {};  // a, b, c, d of one chunk
+    void *d_x[kHostBufs] = {};    // x of one chunk (8 B / eq)
 };
 
 static void host_ctx_free(tprgb_host_ctx *h) {
-    for (int i = 0; i < kHostStreams; i++) {
-        if (h->st[i]) cudaStreamDestroy(h->st[i]);
-        if (h->up[i]) cudaEventDestroy(h->up[i]);
+    for (cudaStream_t s : {h->up, h->solve, h->down})
+        if (s) cudaStreamDestroy(s);
+    for (int i = 0; i < kHostBufs; i++) {
+        for (cudaEvent_t e : {h->uploaded[i], h->solved[i], h->downloaded[i]})
+            if (e) cudaEventDestroy(e);
         cudaFree(h->d_in[i]);
         cudaFree(h->d_x[i]);
     }
     delete h;
+}
+
+static void host_ctx_sync(tprgb_host_ctx *h) {
+    for (cudaStream_t s : {h->up, h->solve, h->down}) cudaStreamSynchronize(s);
 }
 
 extern "C" {
@@ -172,15 +181,19 @@ TPRGB_API int tprgb_host_ctx_create(int64_t chunk_eq, tprgb_host_ctx **out) {
                     (long long)chunk_eq);
     tprgb_host_ctx *h = new tprgb_host_ctx();
     h->chunk_eq = chunk_eq;
-    for (int i = 0; i < kHostStreams; i++) {
-        cudaError_t e = cudaStreamCreateWithFlags(&h->st[i], cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->up[i], cudaEventDisableTiming);
+    cudaError_t e = cudaStreamCreateWithFlags(&h->up, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->solve, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->down, cudaStreamNonBlocking);
+    for (int i = 0; i < kHostBufs && e == cudaSuccess; i++) {
+        e = cudaEventCreateWithFlags(&h->uploaded[i], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->solved[i], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->downloaded[i], cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaMalloc(&h->d_in[i], 4 * sizeof(float) * (size_t)chunk_eq);
         if (e == cudaSuccess) e = cudaMalloc(&h->d_x[i], sizeof(double) * (size_t)chunk_eq);
-        if (e != cudaSuccess) {
-            host_ctx_free(h);
-            return cuda_fail(e, "tprgb_host_ctx_create");
-        }
+    }
+    if (e != cudaSuccess) {
+        host_ctx_free(h);
+        return cuda_fail(e, "tprgb_host_ctx_create");
     }
     *out = h;
     return TPRGB_OK;
@@ -188,7 +201,7 @@ TPRGB_API int tprgb_host_ctx_create(int64_t chunk_eq, tprgb_host_ctx **out) {
 
 TPRGB_API int tprgb_host_ctx_destroy(tprgb_host_ctx *h) {
     if (!h) return fail(TPRGB_EINVAL, "ctx is NULL");
-    for (int i = 0; i < kHostStreams; i++) cudaStreamSynchronize(h->st[i]);
+    host_ctx_sync(h);
     host_ctx_free(h);
     return TPRGB_OK;
 }
@@ -234,26 +247,48 @@ TPRGB_API int tprgb_batch_solve_host(tprgb_host_ctx *h, int nsys, int n,
                 sizes.push_back(std::min<int64_t>(per, nsys - s0));
         }
     }
-    int k = 0;
+    // on an error part-way, the work already queued is drained before
+    // returning, so no copy still targets the caller's arrays
+    auto drained = [&](int rc) {
+        host_ctx_sync(h);
+        return rc;
+    };
     int64_t s0 = 0;
-    for (size_t ci = 0; ci < sizes.size(); ci++, k = (k + 1) % kHostStreams) {
+    for (size_t ci = 0; ci < sizes.size(); ci++) {
+        const int k = (int)(ci % kHostBufs);
+        const bool reuse = ci >= (size_t)kHostBufs;  // buffer k held chunk ci - kHostBufs
         const int64_t ns = sizes[ci];
         const int64_t off = s0 * n, neq = ns * n;
-        cudaStream_t st = h->st[k];
         float *da = h->d_in[k], *db = da + h->chunk_eq, *dc = db + h->chunk_eq,
               *dd = dc + h->chunk_eq;
         const size_t bytes = sizeof(float) * (size_t)neq;
-        TPRGB_CUDA(cudaMemcpyAsync(da, a + off, bytes, cudaMemcpyHostToDevice, st));
-        TPRGB_CUDA(cudaMemcpyAsync(db, b + off, bytes, cudaMemcpyHostToDevice, st));
-        TPRGB_CUDA(cudaMemcpyAsync(dc, c + off, bytes, cudaMemcpyHostToDevice, st));
-        TPRGB_CUDA(cudaMemcpyAsync(dd, d + off, bytes, cudaMemcpyHostToDevice, st));
-        int rc = tprgb_batch_solve((int)ns, n, da, db, dc, dd, h->d_x[k], &o, st);
-        if (rc) return rc;
-        TPRGB_CUDA(cudaMemcpyAsync((char *)x + off * xs, h->d_x[k], xs * (size_t)neq,
-                                   cudaMemcpyDeviceToHost, st));
+        cudaError_t e = cudaSuccess;
+        if (reuse) e = cudaStreamWaitEvent(h->up, h->solved[k], 0);
+        const float *src[4] = {a + off, b + off, c + off, d + off};
+        float *dst[4] = {da, db, dc, dd};
+        for (int i = 0; i < 4 && e == cudaSuccess; i++)
+            e = cudaMemcpyAsync(dst[i], src[i], bytes, cudaMemcpyHostToDevice, h->up);
+        if (e == cudaSuccess) e = cudaEventRecord(h->uploaded[k], h->up);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(h->solve, h->uploaded[k], 0);
+        if (e == cudaSuccess && reuse) e = cudaStreamWaitEvent(h->solve, h->downloaded[k], 0);
+        if (e != cudaSuccess) return drained(cuda_fail(e, "tprgb_batch_solve_host"));
+        int rc = tprgb_batch_solve((int)ns, n, da, db, dc, dd, h->d_x[k], &o, h->solve);
+        if (rc) return drained(rc);
+        e = cudaEventRecord(h->solved[k], h->solve);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(h->down, h->solved[k], 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync((char *)x + off * xs, h->d_x[k], xs * (size_t)neq,
+                                cudaMemcpyDeviceToHost, h->down);
+        if (e == cudaSuccess) e = cudaEventRecord(h->downloaded[k], h->down);
+        if (e != cudaSuccess) return drained(cuda_fail(e, "tprgb_batch_solve_host"));
         s0 += ns;
     }
-    for (int i = 0; i < kHostStreams; i++) TPRGB_CUDA(cudaStreamSynchronize(h->st[i]));
+    cudaError_t first = cudaSuccess;
+    for (cudaStream_t s : {h->up, h->solve, h->down}) {
+        const cudaError_t e = cudaStreamSynchronize(s);
+        if (first == cudaSuccess) first = e;
+    }
+    if (first != cudaSuccess) return cuda_fail(first, "tprgb_batch_solve_host");
     return TPRGB_OK;
 }
 
