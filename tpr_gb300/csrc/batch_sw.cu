@@ -170,6 +170,7 @@ batch_cl(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
     __shared__ __align__(8) uint64_t full;
     __shared__ tile::Smem<NT> sm;
     __shared__ float4 crows[tile::kClusterRowSlots];
+    __shared__ __align__(8) uint64_t rbar[2];  // row barriers, one per parity
     __shared__ int s_ok;
     const int tid = threadIdx.x;
     const unsigned P = cl::size(), p = cl::rank();
@@ -182,9 +183,12 @@ batch_cl(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
 
     if (tid == 0) {
         tma::mbar_init(&full, 1);
+        tma::mbar_init(&rbar[0], 1);
+        tma::mbar_init(&rbar[1], 1);
         tma::fence_barrier_init();
     }
     __syncthreads();
+    cl::sync();  // every CTA's row barriers exist before any part stores rows
     auto issue = [&](long long sys) {  // thread 0 only
         tma::fence_proxy_async();
         tma::mbar_expect_tx(&full, 4u * TILE * 4u);
@@ -225,6 +229,8 @@ batch_cl(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
         tile::Part pc;
         pc.on = 2;
         pc.crows = crows;
+        pc.rbar = rbar;
+        pc.cstatus = stw;
         pc.P = (int)P;
         pc.p = (int)p;
         pc.round = round;
@@ -243,7 +249,9 @@ batch_cl(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
         if (sys_status && ok && !finite) atomicOr(&sys_status[sys], 1u);
         round = pc.round;
     }
-    // no CTA leaves while another may still read its shared memory
+    // no CTA leaves while a part of its cluster may still store rows into
+    // its shared memory (possible only after a row wait timed out: every
+    // part otherwise waits for all rows sent to it)
     cl::sync();
     if (pending && tid == 0) tma::mbar_wait(&full, pend_phase, kWaitLimit);
 }

@@ -7,6 +7,7 @@
 #include "cluster.cuh"
 #include "common.cuh"
 #include "hier.cuh"
+#include "tma.cuh"
 
 namespace tprgb {
 namespace tile {
@@ -38,11 +39,14 @@ constexpr int kClusterRowSlots = 2 * 16 * 2;
 // grid meeting at counter barriers in global scratch (per system: counter,
 // then rows [2 parity][32 parts][8 floats] and edges [2 parity][32 parts][4
 // floats]); on = 2: the parts are the CTAs of one thread-block cluster,
-// exchanging rows through distributed shared memory at cluster barriers
-// (crows: this CTA's kClusterRowSlots-entry row buffer).
+// exchanging rows through distributed shared memory (crows: this CTA's
+// kClusterRowSlots-entry row buffer; rbar: its two row barriers, one per
+// parity; cstatus: timeout record (code, site, detail)).
 struct Part {
     int on, P, p;
     float4 *crows;
+    uint64_t *rbar;
+    unsigned *cstatus;
     unsigned *counter;
     float *rows, *edges;
     unsigned round;
@@ -57,6 +61,7 @@ struct Part {
 };
 
 constexpr int kScratchFloats = 4 + 2 * 32 * 8 + 2 * 32 * 4;  // per system
+constexpr unsigned kRowWaitLimit = 1u << 22;  // polls of a row barrier (~0.3 s)
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
     unsigned v;
@@ -157,12 +162,16 @@ __device__ __forceinline__ void solve(const float (&a)[L], const float (&b)[L],
             // every part solves the 2P-row system redundantly
             const unsigned par = pc.round & 1u;
             if (pc.on == 2) {
-                // lane j stores the rows into CTA j's buffer: remote stores
-                // complete under the barrier, and the level-3 reads after it
-                // are local (a remote read there would put a distributed
-                // shared-memory round trip on every part's critical path).
-                // A parity's slots are rewritten two barriers later, after
-                // every CTA has read them.
+                // lane j stores the two rows into slot p of CTA j's buffer
+                // with st.async, completing 32 bytes on CTA j's row barrier
+                // of this parity; warp 0 then waits (bounded) until all P
+                // parts' rows are in, and reads them locally.  No cluster
+                // barrier: the other warps wait for warp 0 at the CTA
+                // barrier below, and nobody waits for this CTA's earlier
+                // global stores.  Slots and barrier of a parity are reused
+                // two rounds later; a part gets there only after receiving
+                // every part's rows of the round in between, which each
+                // part sends after it has read this round's rows.
                 if (warp == 0) {
                     const float a0 = __shfl_sync(0xffffffffu, S0.a, 0);
                     const float c0 = __shfl_sync(0xffffffffu, S0.c, 0);
@@ -170,14 +179,22 @@ __device__ __forceinline__ void solve(const float (&a)[L], const float (&b)[L],
                     const float a1 = __shfl_sync(0xffffffffu, S1.a, W - 1);
                     const float c1 = __shfl_sync(0xffffffffu, S1.c, W - 1);
                     const float d1 = __shfl_sync(0xffffffffu, S1.d, W - 1);
+                    if (lane == 0) tma::mbar_expect_tx(pc.rbar + par, 32u * (unsigned)pc.P);
                     if (lane < pc.P) {
                         const uint32_t dst =
                             cl::map(pc.crows + (par * 16 + pc.p) * 2, (unsigned)lane);
-                        cl::st4(dst, make_float4(a0, c0, d0, 0.f));
-                        cl::st4(dst + 16u, make_float4(a1, c1, d1, 0.f));
+                        const uint32_t bar = cl::map(pc.rbar + par, (unsigned)lane);
+                        cl::st_async4(dst, make_float4(a0, c0, d0, 0.f), bar);
+                        cl::st_async4(dst + 16u, make_float4(a1, c1, d1, 0.f), bar);
+                    }
+                    const bool in = cl::mbar_wait(pc.rbar + par, (pc.round >> 1) & 1u,
+                                                  kRowWaitLimit);
+                    if (!in && lane == 0) {
+                        atomicCAS(&pc.cstatus[0], 0u, (unsigned)TPRGB_ETIMEOUT);
+                        pc.cstatus[1] = 4;
+                        pc.cstatus[2] = pc.round;
                     }
                 }
-                cl::sync();
                 pc.round++;
             } else {
                 if (warp == 0 && lane == 0) {
