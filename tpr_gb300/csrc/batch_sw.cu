@@ -37,6 +37,33 @@ constexpr int sw_min_blocks(int L, int NT) {
                                                       : 65536 / (NT * (L >= 16 ? 128 : 80));
 }
 
+// Stage-free hook of the one-stage uniform tile: after the tile's last read
+// of the stage (every thread calls it there), thread 0 starts loading the
+// next tile into the same stage, so the load overlaps the rest of the
+// solve and the stores.  Plain values only: a hook that refers to the
+// kernel's locals would put them in local memory.
+struct NextTileLoad {
+    const CUtensorMap *maps;  // a, b, c, d
+    float *stage;
+    uint64_t *bar;
+    unsigned bytes;  // one tile of the four arrays
+    int tile_elems;
+    int row;         // first 128-byte row of the next tile
+    bool use;        // the kernel takes this route (CTA-uniform)
+    bool go;         // this thread issues (thread 0, a next tile exists)
+    __device__ __forceinline__ void operator()() const {
+        if (!use) return;
+        __syncthreads();  // every thread is done reading the stage
+        if (go) {
+            tma::fence_proxy_async();
+            tma::mbar_expect_tx(bar, bytes);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                tma::tensor_g2s_2d(stage + k * tile_elems, &maps[k], 0, row, bar);
+        }
+    }
+};
+
 // Systems at offsets: sys_off (element offsets, multiples of 32, n >= 256)
 // gives system k's first equation; the tensor maps' box is then one system
 // (n / 32 rows) and each tile is G box loads per array, issued by the
@@ -134,14 +161,22 @@ batch_sw(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
         pc.round = 0;
         const float *s0 = stages + st * 4 * TILE;
         const long long sbase = active ? (sys_off ? sys_off[sys] : sys * n) : 0;
+        // one stage, systems back to back: the next tile loads as soon as
+        // this one's last read of the stage is done
+        const bool early = S == 1 && !sys_off;
+        const NextTileLoad hook{tm.m, stages, &full[0], 4u * TILE * 4u, TILE,
+                                (int)((tl + stride) * ROWS), early,
+                                early && tid == 0 && tl + stride < ntiles};
         const bool finite = tile::run_tile_smem<L, NT, T, MODE, true>(
             s0, s0 + TILE, s0 + 2 * TILE, s0 + 3 * TILE, off, gx,
             active ? sbase + (long long)t * L : 0, active, t, t == 0,
-            t == T - 1, refine_steps, x_f64, sm, pc);
+            t == T - 1, refine_steps, x_f64, sm, pc, hook);
         if (sys_status && active && !finite) atomicOr(&sys_status[sys], 1u);
-        __syncthreads();  // every thread is done reading this stage
-        if (tid < 32 && tl + (long long)S * stride < ntiles)
-            issue(tl + (long long)S * stride, st);
+        if (!early) {
+            __syncthreads();  // every thread is done reading this stage
+            if (tid < 32 && tl + (long long)S * stride < ntiles)
+                issue(tl + (long long)S * stride, st);
+        }
     }
 }
 
