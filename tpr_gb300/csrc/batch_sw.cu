@@ -301,17 +301,19 @@ using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t,
                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 static int tensor_encoder(EncodeTiled *out) {
-    static EncodeTiled fn = nullptr;
-    if (!fn) {
+    static std::atomic<EncodeTiled> fn{nullptr};
+    EncodeTiled f = fn.load(std::memory_order_acquire);
+    if (!f) {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
         cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p,
                                                          12000, cudaEnableDefault, &q);
         if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p)
             return fail(TPRGB_EUNSUPPORTED, "cuTensorMapEncodeTiled is not available");
-        fn = reinterpret_cast<EncodeTiled>(p);
+        f = reinterpret_cast<EncodeTiled>(p);
+        fn.store(f, std::memory_order_release);
     }
-    *out = fn;
+    *out = f;
     return TPRGB_OK;
 }
 
@@ -321,16 +323,19 @@ static int launch_sw_t(const BatchArgs &A, int S, cudaStream_t st) {
     constexpr int ROWS = NT * L / 32;
     const size_t smem = (size_t)S * 4 * NT * L * sizeof(float) + 1024;
     auto k = bt::batch_sw<L, NT, T, MODE>;
-    static int grid_cap[3] = {0, 0, 0};
-    if (!grid_cap[S]) {
+    static DeviceOnce grid_cap[3];  // by stage count
+    int dev = 0;
+    TPRGB_CUDA(cudaGetDevice(&dev));
+    int cap = grid_cap[S].get(dev);
+    if (!cap) {
         const size_t smax = 2ull * 4 * NT * L * sizeof(float) + 1024;
         TPRGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smax));
-        int dev = 0, sms = 0, per = 0;
-        TPRGB_CUDA(cudaGetDevice(&dev));
+        int sms = 0, per = 0;
         TPRGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         TPRGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, NT, smem));
-        grid_cap[S] = std::max(1, sms * std::max(per, 1));
+        cap = std::max(1, sms * std::max(per, 1));
+        grid_cap[S].set(dev, cap);
     }
     EncodeTiled enc = nullptr;
     int rc = tensor_encoder(&enc);
@@ -353,7 +358,7 @@ static int launch_sw_t(const BatchArgs &A, int S, cudaStream_t st) {
             return fail(TPRGB_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     }
     const long long ntiles = (A.nsys + G - 1) / G;
-    const int grid = (int)std::min<long long>(ntiles, grid_cap[S]);
+    const int grid = (int)std::min<long long>(ntiles, cap);
     k<<<grid, NT, smem, st>>>(tm, A.x, A.nsys, A.refine_steps, A.x_f64, S, A.sys_off,
                               A.sys_status, A.status);
     TPRGB_CUDA(cudaGetLastError());
@@ -412,13 +417,14 @@ static int launch_cl_t(const BatchArgs &A, int P, cudaStream_t st) {
     constexpr int ROWS = TILE / 32;
     const size_t smem = 4ull * TILE * sizeof(float) + 1024;
     auto k = bt::batch_cl<L, NT, MODE>;
-    static int max_clusters[17] = {0};
-    static bool attrs = false;
-    if (!attrs) {
+    static DeviceOnce attrs, max_clusters[17];  // max_clusters by cluster size
+    int dev = 0;
+    TPRGB_CUDA(cudaGetDevice(&dev));
+    if (!attrs.get(dev)) {
         TPRGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem));
         TPRGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-        attrs = true;
+        attrs.set(dev, 1);
     }
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -432,13 +438,13 @@ static int launch_cl_t(const BatchArgs &A, int P, cudaStream_t st) {
     cfg.stream = st;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (!max_clusters[P]) {
-        int num = 0;
-        TPRGB_CUDA(cudaOccupancyMaxActiveClusters(&num, k, &cfg));
-        if (num < 1)
+    int ncl_max = max_clusters[P].get(dev);
+    if (!ncl_max) {
+        TPRGB_CUDA(cudaOccupancyMaxActiveClusters(&ncl_max, k, &cfg));
+        if (ncl_max < 1)
             return fail(TPRGB_EUNSUPPORTED, "a cluster of %d CTAs of %d threads does not fit",
                         P, NT);
-        max_clusters[P] = num;
+        max_clusters[P].set(dev, ncl_max);
     }
     EncodeTiled enc = nullptr;
     int rc = tensor_encoder(&enc);
@@ -460,7 +466,7 @@ static int launch_cl_t(const BatchArgs &A, int P, cudaStream_t st) {
         if (r != CUDA_SUCCESS)
             return fail(TPRGB_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     }
-    const int ncl = (int)std::min<long long>(A.nsys, max_clusters[P]);
+    const int ncl = (int)std::min<long long>(A.nsys, ncl_max);
     cfg.gridDim = dim3((unsigned)(ncl * P), 1, 1);
     TPRGB_CUDA(cudaLaunchKernelEx(&cfg, k, tm, A.x, A.nsys, A.refine_steps, A.x_f64,
                                   A.sys_off, A.sys_status, A.status));

@@ -110,18 +110,21 @@ static int launch_tma_t(const BatchArgs &A, cudaStream_t st) {
     constexpr int G = NT / T;
     const size_t smem = 2ull * 4 * NT * L * sizeof(float);
     auto k = bt::batch_tma<L, NT, T, MODE>;
-    static int grid_cap = 0;
-    if (!grid_cap) {
+    static DeviceOnce grid_cap;
+    int dev = 0;
+    TPRGB_CUDA(cudaGetDevice(&dev));
+    int cap = grid_cap.get(dev);
+    if (!cap) {
         TPRGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem));
-        int dev = 0, sms = 0, per = 0;
-        TPRGB_CUDA(cudaGetDevice(&dev));
+        int sms = 0, per = 0;
         TPRGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         TPRGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, NT, smem));
-        grid_cap = std::max(1, sms * std::max(per, 1));
+        cap = std::max(1, sms * std::max(per, 1));
+        grid_cap.set(dev, cap);
     }
     const long long ntiles = (A.nsys + G - 1) / G;
-    const int grid = (int)std::min<long long>(ntiles, grid_cap);
+    const int grid = (int)std::min<long long>(ntiles, cap);
     k<<<grid, NT, smem, st>>>(A.a, A.b, A.c, A.d, A.x, A.nsys, A.refine_steps,
                               A.x_f64);
     TPRGB_CUDA(cudaGetLastError());

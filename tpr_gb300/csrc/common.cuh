@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "tpr_gb.h"
 
 #if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ < 1000)
@@ -21,6 +23,22 @@ int cuda_fail(cudaError_t e, const char *what);
         cudaError_t e_ = (call);                               \
         if (e_ != cudaSuccess) return ::tprgb::cuda_fail(e_, #call); \
     } while (0)
+
+// A launcher's one-time per-device value (a grid size from an occupancy
+// query, "attributes set"), shared by every host thread that launches: 0
+// until computed.  Publish it only after the work it stands for (e.g.
+// cudaFuncSetAttribute) is done; two threads may both compute it, which is
+// harmless (the calls are idempotent).
+struct DeviceOnce {
+    static constexpr int kDevices = 16;
+    std::atomic<int> v[kDevices] = {};
+    int get(int dev) const {
+        return dev >= 0 && dev < kDevices ? v[dev].load(std::memory_order_acquire) : 0;
+    }
+    void set(int dev, int value) {
+        if (dev >= 0 && dev < kDevices) v[dev].store(value, std::memory_order_release);
+    }
+};
 
 __host__ __device__ constexpr inline bool is_pow2(long long v) {
     return v > 0 && (v & (v - 1)) == 0;

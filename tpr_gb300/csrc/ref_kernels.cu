@@ -17,6 +17,7 @@
 //    slice CTA -> global workspace, stage 2 in one CTA per system, stage 3
 //    per slice CTA.  Three launches on one stream, no grid sync.
 #include <algorithm>
+#include <mutex>
 
 #include "common.cuh"
 
@@ -549,14 +550,19 @@ static const size_t kFusedSmemLimit = 200 * 1024;
 // Raise a kernel's dynamic shared-memory limit to `smem` unless an earlier
 // call on this device already raised it at least that far (the attribute
 // is per function and device; setting it is a host call that would
-// otherwise cost every launch).  set_to[dev]: the limit set so far.
+// otherwise cost every launch).  set_to: the limit set so far per device.
+// Raising takes a lock, so that two threads asking for different limits
+// cannot leave the smaller one set with the larger one recorded.
 template <typename K>
-static int smem_attr(K k, size_t smem, size_t (&set_to)[16]) {
+static int smem_attr(K k, size_t smem, DeviceOnce &set_to) {
     int dev = 0;
     TPRGB_CUDA(cudaGetDevice(&dev));
-    if (dev >= 0 && dev < 16 && set_to[dev] >= smem) return TPRGB_OK;
+    if ((size_t)set_to.get(dev) >= smem) return TPRGB_OK;
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
+    if ((size_t)set_to.get(dev) >= smem) return TPRGB_OK;
     TPRGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    if (dev >= 0 && dev < 16) set_to[dev] = smem;
+    set_to.set(dev, (int)smem);
     return TPRGB_OK;
 }
 
@@ -621,7 +627,7 @@ static int launch_tpr_kind(int nsys, int n, int s, const T *a, const T *c,
         int threads = std::min(refk::kThreads, std::max(64, n));
         auto k = refk::fused_tpr<T, KIND>;
         {
-            static size_t set_to[16] = {};
+            static DeviceOnce set_to;
             int rc = smem_attr(k, smem, set_to);
             if (rc) return rc;
         }
@@ -637,7 +643,7 @@ static int launch_tpr_kind(int nsys, int n, int s, const T *a, const T *c,
         int threads = std::min(refk::kThreads, std::max(64, s));
         auto k = refk::sliced_stage1<T, KIND>;
         {
-            static size_t set_to[16] = {};
+            static DeviceOnce set_to;
             int rc = smem_attr(k, smem, set_to);
             if (rc) return rc;
         }
@@ -649,7 +655,7 @@ static int launch_tpr_kind(int nsys, int n, int s, const T *a, const T *c,
         int threads = std::min(refk::kThreads, std::max(64, m));
         auto k = refk::sliced_stage2<T, KIND>;
         {
-            static size_t set_to[16] = {};
+            static DeviceOnce set_to;
             int rc = smem_attr(k, smem, set_to);
             if (rc) return rc;
         }
@@ -661,7 +667,7 @@ static int launch_tpr_kind(int nsys, int n, int s, const T *a, const T *c,
         int threads = std::min(refk::kThreads, std::max(64, s));
         auto k = refk::sliced_stage3<T, KIND>;
         if (smem) {
-            static size_t set_to[16] = {};
+            static DeviceOnce set_to;
             int rc = smem_attr(k, smem, set_to);
             if (rc) return rc;
         }
