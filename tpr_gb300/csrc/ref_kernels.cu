@@ -693,7 +693,7 @@ static int launch_ref_t(int kind, int nsys, int n, int s, const T *a,
             int threads = std::min(refk::kThreads, std::max(64, n));
             auto k = kind == TPRGB_CR ? refk::fused_crpcr<T, TPRGB_CR>
                                       : refk::fused_crpcr<T, TPRGB_PCR>;
-            static size_t set_cr[16] = {}, set_pcr[16] = {};
+            static DeviceOnce set_cr, set_pcr;
             int rc = smem_attr(k, smem, kind == TPRGB_CR ? set_cr : set_pcr);
             if (rc) return rc;
             k<<<nsys, threads, smem, st>>>(a, c, r, x, n, stride);
