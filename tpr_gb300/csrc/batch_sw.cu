@@ -183,14 +183,15 @@ batch_sw(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
 // ---- systems spanning a thread-block cluster --------------------------------
 // One cluster of P CTAs per system of n = P * NT * L equations; CTA rank p
 // stages rows [p * ROWS, (p + 1) * ROWS) of the system's 128-byte rows with
-// a swizzled tensor-map load and solves its part; the parts' boundary rows
-// meet in distributed shared memory at cluster barriers (level 3).  Clusters
+// a swizzled tensor-map load and solves its part; each solve's level 3 has
+// every part send its two boundary rows into every part's shared memory
+// (st.async onto a row mbarrier per parity, see tile::solve).  Clusters
 // walk the batch with a stride of the number of clusters; every CTA of a
-// cluster runs the same number of systems and solves, so their cluster
-// barriers pair up.  A load that times out is recorded in the status word,
-// its CTA stores nothing for that system, and the CTA keeps taking part in
-// the barriers.  sys_off / sys_status / status as for batch_sw (offsets
-// multiples of 32).
+// cluster runs the same number of systems and solves, so their row
+// exchanges pair up.  A load that times out is recorded in the status
+// word, its CTA stores nothing for that system, and the CTA keeps taking
+// part in the exchanges.  sys_off / sys_status / status as for batch_sw
+// (offsets multiples of 32).
 template <int L, int NT, int MODE>
 __global__ void __launch_bounds__(NT, sw_min_blocks(L, NT))
 batch_cl(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
@@ -238,7 +239,7 @@ batch_cl(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
     unsigned round = 0;
     // After a load times out, the CTA issues no more loads and solves its
     // remaining parts on placeholder rows (storing nothing), so that its
-    // cluster barriers still pair with the other CTAs'; before leaving it
+    // row exchanges still pair with the other CTAs'; before leaving it
     // waits, bounded, for the late copy.
     bool pending = false;
     unsigned pend_phase = 0;
