@@ -411,6 +411,17 @@ TPRGB_API int tprgb_cusparse_gtsv(int prec, int n, const void *a,
  * bounded wait gave up since the last reset (reset != 0 clears it). */
 TPRGB_API int tprgb_batch_status(unsigned *code, int reset);
 
+/* Runs one kind of the solver kernels' bounded device waits on a condition
+ * that never comes true and reports what it recorded: status[0] = code
+ * (TPRGB_ETIMEOUT when the wait gave up), status[1] = site, status[2] =
+ * detail.  which: 0 the wait for a TMA load (polls: 1 .. 2^22; the
+ * kernels use 2^18, 1.0 s on GB300), 1 the cluster row-exchange wait
+ * (polls as for 0), 2 the global-memory barrier between the CTAs of one
+ * system (its fixed limit, about 1.1 s; polls is ignored).  Nothing
+ * faults; the context stays usable.  Synchronous. */
+TPRGB_API int tprgb_selftest_wait_timeout(int which, unsigned polls,
+                                          unsigned *status);
+
 /* out[i] = hi[i] + lo[i] as the nearest double, computed on the device by
  * the same integer bit assembly the batched solver uses for its FP64
  * output (no reference counterpart; exposed for testing). */

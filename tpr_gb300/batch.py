@@ -38,6 +38,7 @@ def _declare(L):
         "tprgb_tune_set": (i, [i, i, i, i]),
         "tprgb_tune_get": (i, [i, C.POINTER(i), C.POINTER(i), C.POINTER(i)]),
         "tprgb_batch_status": (i, [C.POINTER(C.c_uint), i]),
+        "tprgb_selftest_wait_timeout": (i, [i, C.c_uint, C.POINTER(C.c_uint)]),
         "tprgb_tune_clear": (i, []),
         "tprgb_plan_create": (i, [i, vp, vp, C.POINTER(BatchOpts),
                                   C.POINTER(vp)]),

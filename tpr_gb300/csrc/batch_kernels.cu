@@ -149,3 +149,67 @@ extern "C" TPRGB_API int tprgb_diag_pair_to_double(int64_t n, const float *hi,
     TPRGB_CUDA(cudaGetLastError());
     return TPRGB_OK;
 }
+
+// ---- bounded waits: self-test ------------------------------------------------
+// Each kind of device wait in the solver kernels gives up after a bounded
+// number of polls and reports TPRGB_ETIMEOUT instead of hanging.  This
+// kernel runs one of them on a condition that never comes true (a flag
+// nothing sets), so a test can check the give-up path and that the context
+// stays usable afterwards.  which: 0 the mbarrier wait for a TMA load
+// (tma::mbar_wait), 1 the cluster row-barrier wait (cl::mbar_wait, with
+// cluster-scope acquire), 2 the barrier of a multi-CTA system in global
+// memory (tile::part_barrier, for a system of two parts of which only this
+// one runs).  Nothing faults or traps; the wait just runs out.
+namespace tprgb {
+namespace bk {
+__global__ void selftest_wait_kernel(int which, unsigned polls, DeviceStatus *st,
+                                     unsigned *counter) {
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ tile::Smem<32> sm;
+    if (which == 0 || which == 1) {
+        if (threadIdx.x == 0) {
+            tma::mbar_init(&bar, 1);  // one arrival per phase; none comes
+            tma::fence_barrier_init();
+        }
+        __syncthreads();
+        const bool in = which == 0 ? tma::mbar_wait(&bar, 0, polls)
+                                   : cl::mbar_wait(&bar, 0, polls);
+        if (threadIdx.x == 0 && !in) {
+            st->code = (unsigned)TPRGB_ETIMEOUT;
+            st->where = (unsigned)which;
+        }
+        return;
+    }
+    tile::Part pc{};
+    pc.on = 1;
+    pc.P = 2;
+    pc.p = 0;
+    pc.counter = counter;
+    pc.round = 0;
+    pc.status = st;
+    pc.item = 7;
+    tile::part_barrier<32>(pc, sm, 2);
+}
+}  // namespace bk
+}  // namespace tprgb
+
+extern "C" TPRGB_API int tprgb_selftest_wait_timeout(int which, unsigned polls,
+                                                     unsigned *status) {
+    using namespace tprgb;
+    if (which < 0 || which > 2 || !status) return fail(TPRGB_EINVAL, "bad arguments");
+    if (which < 2 && (polls == 0 || polls > (1u << 22)))
+        return fail(TPRGB_EINVAL, "polls=%u not in 1 .. 2^22", polls);
+    unsigned *d = nullptr;  // DeviceStatus (4 words) then the counter
+    TPRGB_CUDA(cudaMalloc(&d, 8 * sizeof(unsigned)));
+    cudaError_t e = cudaMemset(d, 0, 8 * sizeof(unsigned));
+    if (e == cudaSuccess) {
+        bk::selftest_wait_kernel<<<1, 32>>>(which, polls,
+                                            reinterpret_cast<DeviceStatus *>(d), d + 4);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(status, d, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(e, "tprgb_selftest_wait_timeout");
+    return TPRGB_OK;
+}

@@ -23,7 +23,10 @@ __device__ unsigned g_sw_status[4];  // code, where, tile, unused
 
 namespace bt {
 
-constexpr unsigned kWaitLimit = 1u << 22;  // polls (~0.3 s with back-off)
+// polls of a load's mbarrier before giving up: 1.0 s on GB300 (a poll with
+// its back-off sleep takes about 3.8 us; measured with
+// tprgb_selftest_wait_timeout)
+constexpr unsigned kWaitLimit = 1u << 18;
 
 // ---- tensor-map (swizzled) staging ----------------------------------------
 struct TensorMaps {

@@ -15,7 +15,10 @@ namespace tile {
 using hier::Chunk;
 using hier::Row;
 
-constexpr unsigned kSpinLimit = 1u << 23;  // ~1 s with the back-off below
+// polls of a multi-CTA barrier in global memory before giving up: about
+// 1.1 s on GB300 with the back-off of part_barrier (2^23 polls measured
+// 4.3 s with tprgb_selftest_wait_timeout)
+constexpr unsigned kSpinLimit = 1u << 21;
 
 struct SegRows {
     Row R0, R1;
@@ -61,7 +64,8 @@ struct Part {
 };
 
 constexpr int kScratchFloats = 4 + 2 * 32 * 8 + 2 * 32 * 4;  // per system
-constexpr unsigned kRowWaitLimit = 1u << 22;  // polls of a row barrier (~0.3 s)
+// polls of a cluster row barrier before giving up: 1.0 s on GB300
+constexpr unsigned kRowWaitLimit = 1u << 18;
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
     unsigned v;
