@@ -55,7 +55,7 @@ class ClockSampler:
          "clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index: int, period_ms: int = 50):
+    def __init__(self, index: int, period_ms: int = 20):
         self.index, self.period = index, period_ms
         self.rows, self.proc = [], None
 
@@ -75,17 +75,30 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.rows.append([v.strip() for v in line.split(",")])
 
+    def wait_ready(self, timeout_s: float = 3.0):
+        """Block until the first sample arrived (nvidia-smi takes a moment
+        to start), so that the timed region that follows is sampled."""
+        end = time.time() + timeout_s
+        while self.proc and not self.rows and time.time() < end:
+            time.sleep(0.01)
+
+    def mark(self) -> int:
+        return len(self.rows)
+
     def __exit__(self, *exc):
         if self.proc:
             time.sleep(self.period / 1000.0)
             self.proc.terminate()
             self.proc.wait(timeout=5)
 
-    def summary(self):
+    def summary(self, lo: int = 0, hi: int = None):
+        """Samples taken between mark() lo and mark() hi, plus the nearest
+        one on each side (a short timed region may fall between two)."""
+        hi = len(self.rows) if hi is None else hi
         mhz, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
                  "sw_power_cap"]
-        for r in self.rows:
+        for r in self.rows[max(0, lo - 1):hi + 1]:
             try:
                 mhz.append(float(r[0]))
                 mx = float(r[1])
@@ -228,6 +241,8 @@ def run_ours(args):
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
+        clk.wait_ready()
+        m0 = clk.mark()
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
         t0.record(stream)
@@ -237,6 +252,7 @@ def run_ours(args):
             evs[i][1].record(stream)
         t1.record(stream)
         torch.cuda.synchronize()
+        m1 = clk.mark()
         if dist:
             dist.barrier()
         total_ms = t0.elapsed_time(t1)
@@ -316,7 +332,7 @@ def run_ours(args):
                     "h2d_bytes_per_step": 16 * NSYS * N,
                     "d2h_bytes_per_step": 8 * NSYS * N},
             "gpu_launches": args.steps,
-            "clocks": clk.summary(),
+            "clocks": clk.summary(m0, m1),
         }
         if cpu:
             line["cpu_baseline"] = cpu
@@ -329,7 +345,7 @@ def run_ours(args):
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--steps", type=int, default=2000)
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cpu-seconds", type=float, default=10.0)
