@@ -121,3 +121,23 @@ def test_pm_cli_usage_and_unknown_solver(capsys):
     assert "Usage" in capsys.readouterr().err
     with pytest.raises(SystemExit):
         pm.run(64, 8, 1, "lapack")
+
+
+def test_bench_clock_window():
+    """bench.py's clock summary covers the samples taken between two marks
+    plus the nearest one on each side, and reports throttle reasons seen
+    there only."""
+    import bench
+    clk = bench.ClockSampler(0)
+    idle = ["2070", "2070", "500", "Not Active", "Not Active", "Not Active",
+            "Not Active", "Not Active"]
+    hot = ["1900", "2070", "1300", "Active", "Not Active", "Not Active",
+           "Not Active", "Active"]
+    clk.rows = [idle, idle, hot, hot, hot, idle, idle]
+    s = clk.summary(3, 4)             # rows 2..4 (one before, one after)
+    assert s["samples"] == 3
+    assert s["sm_mhz"] == 1900.0 and s["sm_max_mhz"] == 2070.0
+    assert s["reasons"] == ["sw_power_cap"]
+    s = clk.summary(6, 6)             # a window between two samples
+    assert s["samples"] == 2 and s["reasons"] == []
+    assert clk.summary()["samples"] == 7
