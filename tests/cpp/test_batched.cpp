@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <thread>
 #include <vector>
 
 #include "tpr_gb.hpp"
@@ -93,8 +94,62 @@ static void expect(const char *name, double worst) {
     if (!ok) failures++;
 }
 
+// Uploads a batch, solves it on `stream` through the C++ wrapper, returns
+// the worst error (1.0 when a call fails).  Device buffers are this call's.
+static double device_solve(const Batch &bt, int n, const tprgb::BatchOptions &o,
+                           cudaStream_t stream) {
+    float *dv[4] = {};
+    double *dx = nullptr;
+    const size_t fb = sizeof(float) * (size_t)bt.neq;
+    const std::vector<float> *hv[4] = {&bt.a, &bt.b, &bt.c, &bt.d};
+    double worst = 1.0;
+    bool ok = cudaMalloc(&dx, sizeof(double) * bt.neq) == cudaSuccess;
+    for (int i = 0; i < 4 && ok; i++)
+        ok = cudaMalloc(&dv[i], fb) == cudaSuccess &&
+             cudaMemcpyAsync(dv[i], hv[i]->data(), fb, cudaMemcpyHostToDevice, stream) ==
+                 cudaSuccess;
+    if (ok) {
+        try {
+            tprgb::batch_solve((int)bt.ns.size(), n, dv[0], dv[1], dv[2], dv[3], dx, o, stream);
+            std::vector<double> x(bt.neq);
+            if (cudaMemcpyAsync(x.data(), dx, sizeof(double) * bt.neq, cudaMemcpyDeviceToHost,
+                                stream) == cudaSuccess &&
+                cudaStreamSynchronize(stream) == cudaSuccess)
+                worst = worst_error(bt, x.data());
+        } catch (const tprgb::Error &) {
+        }
+    }
+    for (int i = 0; i < 4; i++) cudaFree(dv[i]);
+    cudaFree(dx);
+    return worst;
+}
+
 int main() {
     try {
+        // first launches of four kernels at once from four host threads (the
+        // launchers' one-time attribute and occupancy setup runs concurrently)
+        {
+            const int sizes[4] = {1024, 8192, 16384, 2048};
+            const int nsys[4] = {64, 8, 4, 32};
+            std::vector<Batch> bts;
+            for (int i = 0; i < 4; i++)
+                bts.push_back(make_batch(std::vector<int>(nsys[i], sizes[i]), 31 + i));
+            double worst[4] = {1, 1, 1, 1};
+            std::vector<std::thread> th;
+            for (int i = 0; i < 4; i++)
+                th.emplace_back([&, i]() {
+                    cudaStream_t s = nullptr;
+                    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+                        return;
+                    worst[i] = device_solve(bts[i], sizes[i], tprgb::BatchOptions(), s);
+                    cudaStreamDestroy(s);
+                });
+            for (auto &t : th) t.join();
+            const char *names[4] = {"4 threads: first launch n=1024", "4 threads: first launch n=8192",
+                                    "4 threads: first launch n=16384",
+                                    "4 threads: first launch n=2048"};
+            for (int i = 0; i < 4; i++) expect(names[i], worst[i]);
+        }
         // uniform batch through the host pipeline (two calls, one context)
         {
             Batch bt = make_batch(std::vector<int>(300, 1024), 7);

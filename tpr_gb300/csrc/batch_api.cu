@@ -1,5 +1,6 @@
 // C ABI of the batched solver: options, tile selection, uniform batches.
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "batch.cuh"
@@ -21,12 +22,19 @@ TileConfig default_tile(int n) {
 }
 
 // Tuned tiles per log2(n) (set by the autotuner through tprgb_tune_set).
+// Read on every launch, possibly from the serving thread while another
+// thread sets the table: a lock (uncontended in steady state) keeps each
+// read whole.
+static std::mutex g_tuned_mu;
 static TileConfig g_tuned[32];
 static bool g_has_tuned[32];
 
 TileConfig tuned_tile(int n) {
     int k = ilog2(n);
-    if (k >= 0 && k < 32 && g_has_tuned[k]) return g_tuned[k];
+    {
+        std::lock_guard<std::mutex> lk(g_tuned_mu);
+        if (k >= 0 && k < 32 && g_has_tuned[k]) return g_tuned[k];
+    }
     return default_tile(n);
 }
 
@@ -59,6 +67,7 @@ TPRGB_API int tprgb_tune_set(int n, int eq_per_thread, int threads_per_cta,
     int rc = batch_config_check(n, c);  // cluster tiles: cluster_parts' rules
     if (rc) return rc;
     int k = ilog2(n);
+    std::lock_guard<std::mutex> lk(g_tuned_mu);
     g_tuned[k] = c;
     g_has_tuned[k] = true;
     return TPRGB_OK;
@@ -75,6 +84,7 @@ TPRGB_API int tprgb_tune_get(int n, int *eq_per_thread, int *threads_per_cta,
 }
 
 TPRGB_API int tprgb_tune_clear(void) {
+    std::lock_guard<std::mutex> lk(g_tuned_mu);
     for (int k = 0; k < 32; k++) g_has_tuned[k] = false;
     return TPRGB_OK;
 }
