@@ -67,13 +67,41 @@ struct NextTileLoad {
     }
 };
 
+// The same for systems at offsets (plans, serving steps): the next tile's
+// systems are loaded by the lanes of warp 0, one box of N / 32 rows per
+// system and array, as at the top of the tile loop.
+template <int TILE, int N>
+struct NextTileLoadOffsets {
+    const CUtensorMap *maps;  // a, b, c, d
+    float *stage;
+    uint64_t *bar;
+    const long long *sys_off;
+    long long s0;  // first system of the next tile
+    int gs;        // systems in the next tile
+    bool go;       // this thread's warp issues: a next tile exists
+    __device__ __forceinline__ void operator()() const {
+        __syncthreads();  // every thread is done reading the stage
+        if (!go) return;
+        const int lane = threadIdx.x & 31;
+        tma::fence_proxy_async();
+        if (lane == 0) tma::mbar_expect_tx(bar, 4u * (unsigned)gs * N * 4u);
+        __syncwarp();
+        for (int g = lane; g < gs; g += 32) {
+            const int r = (int)(sys_off[s0 + g] >> 5);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                tma::tensor_g2s_2d(stage + k * TILE + g * N, &maps[k], 0, r, bar);
+        }
+    }
+};
+
 // Systems at offsets: sys_off (element offsets, multiples of 32, n >= 256)
 // gives system k's first equation; the tensor maps' box is then one system
 // (n / 32 rows) and each tile is G box loads per array, issued by the
 // lanes of warp 0.  sys_off == nullptr: system k at k * n, one box per tile.
 // sys_status (may be null): word k |= 1 when system k's solution is not
 // finite.  status: timeout record (code, site, detail), g_sw_status if null.
-template <int L, int NT, int T, int MODE>
+template <int L, int NT, int T, int MODE, bool OFFS_HOOK>
 __global__ void __launch_bounds__(NT, sw_min_blocks(L, NT))
 batch_sw(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
          int refine_steps, int x_f64, int S, const long long *__restrict__ sys_off,
@@ -164,16 +192,29 @@ batch_sw(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
         pc.round = 0;
         const float *s0 = stages + st * 4 * TILE;
         const long long sbase = active ? (sys_off ? sys_off[sys] : sys * n) : 0;
-        // one stage, systems back to back: the next tile loads as soon as
-        // this one's last read of the stage is done
-        const bool early = S == 1 && !sys_off;
-        const NextTileLoad hook{tm.m, stages, &full[0], 4u * TILE * 4u, TILE,
-                                (int)((tl + stride) * ROWS), early,
-                                early && tid == 0 && tl + stride < ntiles};
-        const bool finite = tile::run_tile_smem<L, NT, T, MODE, true>(
-            s0, s0 + TILE, s0 + 2 * TILE, s0 + 3 * TILE, off, gx,
-            active ? sbase + (long long)t * L : 0, active, t, t == 0,
-            t == T - 1, refine_steps, x_f64, sm, pc, hook);
+        // one stage: the next tile loads as soon as this one's last read of
+        // the stage is done (OFFS_HOOK: the instance for systems at offsets,
+        // launched with S = 1 only; otherwise systems back to back)
+        const bool early = OFFS_HOOK || (S == 1 && !sys_off);
+        bool finite;
+        if constexpr (OFFS_HOOK) {
+            const long long nx = tl + stride;
+            const NextTileLoadOffsets<TILE, n> hook{
+                tm.m, stages, &full[0], sys_off, nx * G,
+                (int)min((long long)G, (long long)nsys - nx * G), tid < 32 && nx < ntiles};
+            finite = tile::run_tile_smem<L, NT, T, MODE, true>(
+                s0, s0 + TILE, s0 + 2 * TILE, s0 + 3 * TILE, off, gx,
+                active ? sbase + (long long)t * L : 0, active, t, t == 0,
+                t == T - 1, refine_steps, x_f64, sm, pc, hook);
+        } else {
+            const NextTileLoad hook{tm.m, stages, &full[0], 4u * TILE * 4u, TILE,
+                                    (int)((tl + stride) * ROWS), early,
+                                    early && tid == 0 && tl + stride < ntiles};
+            finite = tile::run_tile_smem<L, NT, T, MODE, true>(
+                s0, s0 + TILE, s0 + 2 * TILE, s0 + 3 * TILE, off, gx,
+                active ? sbase + (long long)t * L : 0, active, t, t == 0,
+                t == T - 1, refine_steps, x_f64, sm, pc, hook);
+        }
         if (sys_status && active && !finite) atomicOr(&sys_status[sys], 1u);
         if (!early) {
             __syncthreads();  // every thread is done reading this stage
@@ -321,12 +362,12 @@ static int tensor_encoder(EncodeTiled *out) {
     return TPRGB_OK;
 }
 
-template <int L, int NT, int T, int MODE>
-static int launch_sw_t(const BatchArgs &A, int S, cudaStream_t st) {
+template <int L, int NT, int T, int MODE, bool OFFS_HOOK>
+static int launch_sw_k(const BatchArgs &A, int S, cudaStream_t st) {
     constexpr int G = NT / T;
     constexpr int ROWS = NT * L / 32;
     const size_t smem = (size_t)S * 4 * NT * L * sizeof(float) + 1024;
-    auto k = bt::batch_sw<L, NT, T, MODE>;
+    auto k = bt::batch_sw<L, NT, T, MODE, OFFS_HOOK>;
     static DeviceOnce grid_cap[3];  // by stage count
     int dev = 0;
     TPRGB_CUDA(cudaGetDevice(&dev));
@@ -367,6 +408,19 @@ static int launch_sw_t(const BatchArgs &A, int S, cudaStream_t st) {
                               A.sys_status, A.status);
     TPRGB_CUDA(cudaGetLastError());
     return TPRGB_OK;
+}
+
+// Systems at offsets with one stage get the instance that loads the next
+// tile early where plans and serving steps use it: 16 equations per
+// thread, one system per CTA (n = 1024, 2048, 4096 on 64, 128, 256
+// threads), refined.  Other shapes load after the tile (with several
+// systems per CTA the early-load instance spilled 4-24 bytes).
+template <int L, int NT, int T, int MODE>
+static int launch_sw_t(const BatchArgs &A, int S, cudaStream_t st) {
+    if constexpr (L == 16 && T == NT && MODE == 1) {
+        if (A.sys_off && S == 1) return launch_sw_k<L, NT, T, MODE, true>(A, S, st);
+    }
+    return launch_sw_k<L, NT, T, MODE, false>(A, S, st);
 }
 
 template <int L, int NT, int T>
