@@ -5,6 +5,8 @@ import glob
 import os
 import re
 
+import pytest
+
 from tests.conftest import ROOT
 
 
@@ -58,3 +60,27 @@ def test_error_paths_without_gpu(lib):
     assert lib.tprgb_ref_solve_device(0, 1, 1024, 4, 0, None, None, None, None,
                                       None, 0, None) == EINVAL
     assert b"null device pointer" in lib.tprgb_last_error()
+
+
+def test_cpp_sources_compile_against_headers(tmp_path):
+    """The C++ drop-in headers and the C++ test programs compile (syntax and
+    types) without a GPU, so a header change that breaks a caller shows up
+    on CPU already."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    cuda_inc = None
+    for root in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if root and os.path.exists(os.path.join(root, "include", "cuda_runtime.h")):
+            cuda_inc = os.path.join(root, "include")
+    if not gxx or not cuda_inc:
+        pytest.skip("g++ or the CUDA headers are absent")
+    cpp = os.path.join(ROOT, "tests", "cpp")
+    for name in sorted(os.listdir(cpp)):
+        if not name.endswith(".cpp"):
+            continue
+        r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-Wall",
+                            "-I" + os.path.join(ROOT, "include"), "-I" + cuda_inc,
+                            os.path.join(cpp, name)],
+                           capture_output=True, text=True, timeout=120)
+        assert r.returncode == 0, f"{name}:\n{r.stderr}"
