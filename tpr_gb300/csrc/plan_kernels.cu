@@ -448,14 +448,17 @@ static int plan_launch(Plan *p, const float *a, const float *b, const float *c,
         A.total_eq = p->total_eq;
         cudaStream_t rs = fork ? p->side[ri++ % nsides] : st;
         rc = r.kind == 2 ? launch_batch_cl(A, r.cfg, rs) : launch_batch_sw(A, r.cfg, rs);
-        if (rc) return rc;
+        if (rc) break;
     }
+    // join even after a failed launch, so the caller's stream still orders
+    // after whatever was launched on the side streams
     if (fork) {
         for (int i = 0; i < nsides; i++) {
             TPRGB_CUDA(cudaEventRecord(p->join[i], p->side[i]));
             TPRGB_CUDA(cudaStreamWaitEvent(st, p->join[i], 0));
         }
     }
+    if (rc) return rc;
     return launch_persistent(p->nt, plan_mode(*p), p->grid, a, b, c, d, x,
                              p->d_items, p->nitems, p->d_off, p->d_ctl,
                              p->d_scratch, p->refine_steps, p->x_f64, st);

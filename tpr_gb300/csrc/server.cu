@@ -382,14 +382,17 @@ static int launch_step(Server *s) {
         A.total_eq = s->cap_eq;
         cudaStream_t rs = fork ? s->side[ri++ % nsides] : cs;
         rc = r.kind == 2 ? launch_batch_cl(A, r.cfg, rs) : launch_batch_sw(A, r.cfg, rs);
-        if (rc) return rc;
+        if (rc) break;
     }
+    // join even after a failed launch, so the step stream still orders
+    // after whatever was launched on the side streams
     if (fork) {
         for (int i = 0; i < nsides; i++) {
             TPRGB_CUDA(cudaEventRecord(s->join_ev[i], s->side[i]));
             TPRGB_CUDA(cudaStreamWaitEvent(cs, s->join_ev[i], 0));
         }
     }
+    if (rc) return rc;
     int grid = std::max(1, std::min(s->grid, (int)items.size()));
     rc = launch_persistent(s->o.threads_per_cta, s->mode, grid, s->A, s->B,
                            s->Cc, s->D, s->X, b.items, (int)items.size(), b.off,
