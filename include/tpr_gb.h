@@ -223,7 +223,9 @@ TPRGB_API int tprgb_host_ctx_destroy(tprgb_host_ctx *ctx);
 
 /* Uniform batch from host arrays (system k at element k*n) into host x
  * (double or float per opts->x_f64).  Synchronous.  Host arrays should be
- * pinned (cudaHostAlloc / cudaHostRegister) for full copy bandwidth. */
+ * pinned (cudaHostAlloc / cudaHostRegister) for full copy bandwidth; with
+ * a, b, c, d at one spacing in one allocation each chunk is uploaded by
+ * one 2D copy (fewer copies, faster), otherwise by four. */
 TPRGB_API int tprgb_batch_solve_host(tprgb_host_ctx *ctx, int nsys, int n,
                                      const float *a, const float *b,
                                      const float *c, const float *d, void *x,

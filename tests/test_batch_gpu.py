@@ -240,7 +240,9 @@ def test_empty_batch_is_a_no_op(cuda, v, n, L, nt):
 def test_host_pipeline_matches_device_solve(cuda, nsys, chunk_systems):
     """tprgb_batch_solve_host (host arrays, chunks ramped 1/8, 1/4, 1/2 of a
     full chunk at both ends over three streams; small batches in equal
-    chunks) gives the same bits as the device-resident solve."""
+    chunks) gives the same bits as the device-resident solve, with the four
+    arrays separate, in one block at equal spacing (one 2D upload per
+    chunk, pinned or pageable) and in one block at unequal spacing."""
     import torch
     n = 1024
     bt = G.uniform_batch(nsys, n, 4242 + nsys, "uneven")
@@ -252,3 +254,23 @@ def test_host_pipeline_matches_device_solve(cuda, nsys, chunk_systems):
         x.zero_()
         ctx.solve(nsys, n, *pin, x, B.opts(refine_steps=1))
         np.testing.assert_array_equal(x.numpy(), want)
+    # a, b, c, d one after the other in one block (pinned, then pageable):
+    # each chunk uploads with one 2D copy; same bits
+    neq = nsys * n
+    blk = torch.empty(4 * neq, dtype=torch.float32).pin_memory()
+    for i, v in enumerate((bt.a, bt.b, bt.c, bt.d)):
+        blk[i * neq:(i + 1) * neq].copy_(torch.from_numpy(v))
+    for block in (blk, blk.numpy().copy()):
+        views = [block[i * neq:(i + 1) * neq] for i in range(4)]
+        x.zero_()
+        ctx.solve(nsys, n, *views, x, B.opts(refine_steps=1))
+        np.testing.assert_array_equal(x.numpy(), want)
+    # one block at unequal spacing: four copies per chunk, same bits
+    gaps = (0, neq + 16, 2 * neq + 48, 3 * neq + 64)
+    blk2 = np.zeros(4 * neq + 64, dtype=np.float32)
+    views = [blk2[g:g + neq] for g in gaps]
+    for v, src in zip(views, (bt.a, bt.b, bt.c, bt.d)):
+        v[:] = src
+    x.zero_()
+    ctx.solve(nsys, n, *views, x, B.opts(refine_steps=1))
+    np.testing.assert_array_equal(x.numpy(), want)
