@@ -297,8 +297,11 @@ TPRGB_API int tprgb_batch_solve_host(tprgb_host_ctx *h, int nsys, int n,
         if (one_copy && e == cudaSuccess) {
             e = cudaMemcpy2DAsync(da, sizeof(float) * (size_t)h->chunk_eq, a + off,
                                   (size_t)spacing, bytes, 4, cudaMemcpyHostToDevice, h->up);
-            if (e == cudaErrorInvalidValue || e == cudaErrorInvalidPitchValue) {
-                cudaGetLastError();  // refused before anything was queued
+            if (e != cudaSuccess) {
+                // refused before anything was queued (invalid value on this
+                // driver): four copies from here on; an error that is not
+                // the layout's fails those copies too and is reported
+                cudaGetLastError();
                 one_copy = false;
                 e = cudaSuccess;
             }
