@@ -141,3 +141,17 @@ def test_bench_clock_window():
     s = clk.summary(6, 6)             # a window between two samples
     assert s["samples"] == 2 and s["reasons"] == []
     assert clk.summary()["samples"] == 7
+
+
+def test_bench_reads_committed_profile_and_peak():
+    """bench.py takes roofline.traffic from the committed ncu summary of the
+    bench kernel and the peak from the measured-peaks file; both parse, and
+    the traffic is the kernel's DRAM bytes (no more than the algorithmic
+    24 B per equation, no less than the 16 B of inputs it must read)."""
+    import bench
+    traffic = bench.profiled_traffic()
+    assert traffic is not None
+    eq = 16384 * 1024
+    assert 16 * eq <= traffic <= 24 * eq, traffic
+    peak, kind = bench.measured_peak()
+    assert peak > 1000 and kind in ("measured", "fallback")
