@@ -1,4 +1,6 @@
-// Uniform batches staged by swizzled 2D tensor-map loads.
+// Batches staged by swizzled 2D tensor-map loads: batch_sw (one CTA per
+// tile of whole systems) and batch_cl (one thread-block cluster per system,
+// the parts exchanging their level-3 rows in distributed shared memory).
 //
 // Each array's tile is one box of a 2D tensor map (rows of 128 bytes, 32
 // floats) loaded with the 128-byte swizzle: unit u (16 bytes) of row r
@@ -6,8 +8,10 @@
 // chunks' units spread over all 32 banks (a contiguous layout puts lanes
 // whose chunks are 32 or 64 bytes apart on the same banks).  Persistent
 // CTAs walk the batch with a one- or two-stage ring; 8 or 16 equations per
-// thread.  Every mbarrier wait is bounded; a timeout is recorded in this
-// unit's status word and the CTA stops after draining its copies.
+// thread.  Every mbarrier wait is bounded; a timeout is recorded in the
+// status word.  A batch_sw CTA then stops after draining its copies; a
+// batch_cl CTA keeps taking part in its cluster's row exchanges on
+// placeholder rows, storing nothing.
 #include <cuda.h>  // CUtensorMap and its enums (the encoder is fetched at run time)
 
 #include <algorithm>
