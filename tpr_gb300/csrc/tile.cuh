@@ -1,7 +1,9 @@
-// Tile solver shared by the uniform batched kernel and the persistent
-// queue kernel: a CTA of NT threads solves either several whole systems
-// (T = n / L threads each) or one part of a system that spans several CTAs
-// (then the CTAs exchange their boundary rows through global scratch).
+// Tile solver shared by the batched kernels and the persistent queue
+// kernel: a CTA of NT threads solves either several whole systems (T = n / L
+// threads each) or one part of a system that spans several CTAs.  The parts
+// exchange their boundary rows through global scratch at counter barriers
+// (queue kernel) or through distributed shared memory with st.async onto
+// each part's row mbarriers (thread-block clusters).
 #pragma once
 
 #include "cluster.cuh"
