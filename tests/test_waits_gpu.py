@@ -6,6 +6,7 @@ site, and leave the context usable: a batch solved right after still meets
 the refined solver's 1e-9 bound.  Nothing faults or hangs; the waits just
 run out (the third after its fixed limit of about a second)."""
 import ctypes
+import time
 
 import pytest
 
@@ -19,7 +20,11 @@ pytestmark = pytest.mark.gpu
 @pytest.mark.parametrize("which,site,detail", [(0, 0, 0), (1, 1, 0), (2, 2, 7)])
 def test_wait_gives_up_and_reports(cuda, port, which, site, detail):
     st = (ctypes.c_uint * 3)()
+    t0 = time.perf_counter()
     assert T.load().tprgb_selftest_wait_timeout(which, 1 << 14, st) == T.OK
+    waited = time.perf_counter() - t0
+    # 2^14 polls: about 0.06 s; the global barrier's fixed limit: about 1.1 s
+    assert waited < 5.0, waited
     assert st[0] == T.ETIMEOUT
     assert st[1] == site
     assert st[2] == detail
