@@ -12,6 +12,8 @@
  *   - orc_batch_*: OpenMP over independent systems, one private workspace
  *     per thread -- the pattern of the reference's multi-thread test
  *     (test/examples.cpp:130-154) -- used as the timed CPU baseline.
+ *   - orc_time_plain_*: the reference's timed single-system loop
+ *     (src/pm.cpp:160-194) with its solver-internal OpenMP.
  *   - orc_rel_l2: ||x - xt||_2 / ||xt||_2 accumulated in FP64, the
  *     reference's stability metric (src/numerical_stability.cpp:100-115).
  *
@@ -22,9 +24,21 @@
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
+
+/* Monotonic wall clock in seconds. */
+static double orc_now(void) {
+#ifdef _OPENMP
+    return omp_get_wtime();
+#else
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+#endif
+}
 
 /* floor(log2(v)) for v >= 1 (src/lib.hpp:69-91). */
 static int orc_ilog2(int v) {
@@ -155,8 +169,11 @@ void orc_batch_tpr_f32(int kind, int nsys, int n, int s, const float *a,
                        float *x, int nthreads) {
 #pragma omp parallel num_threads(nthreads > 0 ? nthreads : 1)
     {
-        float *wa = (float *)malloc(sizeof(float) * (size_t)n * 3);
-        float *wc = wa + n, *wr = wa + 2 * n;
+        /* one solver object per thread: its workspace is allocated once,
+         * as the reference's init does (src/ptpr.cpp:54-96) */
+        size_t wsz = kind == 0 ? orc_ptpr_ws_size_f32(n, s) : orc_tpr_ws_size_f32(n, s);
+        float *wa = (float *)malloc(sizeof(float) * ((size_t)n * 3 + wsz));
+        float *wc = wa + n, *wr = wa + 2 * n, *ws = wa + 3 * n;
 #pragma omp for schedule(static)
         for (int k = 0; k < nsys; k++) {
             size_t o = (size_t)k * (size_t)n;
@@ -165,9 +182,9 @@ void orc_batch_tpr_f32(int kind, int nsys, int n, int s, const float *a,
             memcpy(wr, d + o, sizeof(float) * (size_t)n);
             orc_normalize_f32(n, wa, b + o, wc, wr);
             if (kind == 0)
-                orc_ptpr_f32(n, s, wa, wc, wr, x + o);
+                orc_ptpr_ws_f32(n, s, wa, wc, wr, x + o, ws);
             else
-                orc_tpr_f32(n, s, wa, wc, wr, x + o);
+                orc_tpr_ws_f32(n, s, wa, wc, wr, x + o, ws);
         }
         free(wa);
     }

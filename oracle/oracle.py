@@ -21,7 +21,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 _PORT = os.path.join(HERE, "liboracle.so")
 _REF = {"f32": os.path.join(HERE, "_ref", "libtprref_f32.so"),
         "f64": os.path.join(HERE, "_ref", "libtprref_f64.so")}
-REFERENCE_ROOT = "/root/reference"
+# The reference tree (read only; used to build oracle/_ref and to make the
+# golden fixtures): $TPR_REFERENCE_ROOT, else a `reference` directory beside
+# this repository's root.
+REFERENCE_ROOT = os.environ.get(
+    "TPR_REFERENCE_ROOT",
+    os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 _fp = C.c_void_p
 _i = C.c_int
@@ -71,6 +76,10 @@ class Port:
         L.orc_batch_tpr_f32.argtypes = [_i, _i, _i, _i, _fp, _fp, _fp, _fp,
                                         _fp, _i]
         L.orc_max_threads.restype = _i
+        for sfx in ("f32", "f64"):
+            fn = getattr(L, f"orc_time_plain_{sfx}")
+            fn.argtypes = [_i, _i, _i, _fp, _fp, _fp, _i, _i, _fp]
+            fn.restype = C.c_double
 
     # -- reference solver restatements (inputs copied, never mutated) -----
     @staticmethod
@@ -167,6 +176,20 @@ class Port:
     def max_threads(self) -> int:
         return int(self.lib.orc_max_threads())
 
+    def time_plain(self, kind, a, c, rhs, s, iters, threads=0,
+                   dtype=np.float32):
+        """The reference's timed single-system loop (src/pm.cpp:160-194)
+        on the diag-normalised a, c, rhs: PTPR (kind 0) or TPR (kind 1)
+        with solver-internal OpenMP on `threads` threads.  Returns (seconds
+        in solve + get_ans over all iterations, last x)."""
+        a, c, rhs = self._prep(dtype, a, c, rhs)
+        x = np.zeros(len(a), dtype)
+        sfx = "f32" if dtype == np.float32 else "f64"
+        t = getattr(self.lib, f"orc_time_plain_{sfx}")(
+            kind, len(a), s, _ptr(a), _ptr(c), _ptr(rhs), iters,
+            threads or os.cpu_count(), _ptr(x))
+        return float(t), x
+
 
 class Ref:
     """The reference's own CPU solvers (built from its sources)."""
@@ -182,6 +205,9 @@ class Ref:
         L.ref_pcr.argtypes = [_i, _fp, _fp, _fp, _fp]
         L.ref_batch_ptpr.argtypes = [_i, _i, _i, _fp, _fp, _fp, _fp, _fp, _i]
         L.ref_batch_tpr.argtypes = [_i, _i, _i, _fp, _fp, _fp, _fp, _fp, _i]
+        for f in ("ref_time_plain_ptpr", "ref_time_plain_tpr"):
+            getattr(L, f).argtypes = [_i, _i, _fp, _fp, _fp, _i, _i, _fp]
+            getattr(L, f).restype = C.c_double
         for f in ("ref_ptpr", "ref_ptpr_diag", "ref_tpr", "ref_cr", "ref_pcr"):
             getattr(L, f).restype = _i
         assert L.ref_real_size() == np.dtype(self.dtype).itemsize
@@ -206,6 +232,17 @@ class Ref:
 
     def pcr(self, a, c, rhs):
         return self._run(self.lib.ref_pcr, a, c, rhs)
+
+    def time_plain(self, kind, a, c, rhs, s, iters, threads=0):
+        """tpr_pm's timed loop on the reference's own PTPR (kind 0) / TPR
+        (kind 1); returns (seconds, last x) like Port.time_plain."""
+        a, c, rhs = [np.array(v, self.dtype, copy=True) for v in (a, c, rhs)]
+        x = np.zeros(len(a), self.dtype)
+        fn = self.lib.ref_time_plain_ptpr if kind == 0 else \
+            self.lib.ref_time_plain_tpr
+        t = fn(len(a), s, _ptr(a), _ptr(c), _ptr(rhs), iters,
+               threads or os.cpu_count(), _ptr(x))
+        return float(t), x
 
     def batch(self, kind, nsys, n, s, a, b, c, d, threads=0):
         x = np.empty(nsys * n, self.dtype)

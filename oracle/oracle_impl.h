@@ -210,8 +210,66 @@ size_t OFN(orc_ptpr_ws_size_)(int n, int s) {
     return (size_t)(3 * s + 9 * m + n + 1);
 }
 
-int OFN(orc_ptpr_ws_)(int n, int s, REAL *a, REAL *c, REAL *rhs, REAL *x,
-                      REAL *ws) {
+/* Stage 1 of one slice [st, st + s): log2(s) PCR-like steps through the
+ * s-sized scratch aa/cc/rr, the E_st backup, the E_st update
+ * (src/ptpr.cpp:130-213). */
+static void OFN(ptpr_st1_slice_)(int s, int ls, int st, REAL *a, REAL *c,
+                                 REAL *rhs, REAL *aa, REAL *cc, REAL *rr,
+                                 REAL *ba, REAL *bc, REAL *br) {
+    int ed = st + s - 1;
+    /* three range loops (rows without a left partner, interior rows, rows
+     * without a right partner), each elementwise so that it vectorises as
+     * the reference's does; the per-row arithmetic is the same */
+    for (int p = 1; p <= ls; p++) {
+        int u = 1 << (p - 1);
+#pragma omp simd
+        for (int i = st; i < st + u; i++)
+            OFN(upd_upper_)(a, c, rhs, i, i + u, &aa[i - st], &cc[i - st],
+                            &rr[i - st]);
+#pragma omp simd
+        for (int i = st + u; i <= ed - u; i++)
+            OFN(upd_mid_)(a, c, rhs, i - u, i, i + u, &aa[i - st],
+                          &cc[i - st], &rr[i - st]);
+#pragma omp simd
+        for (int i = ed - u + 1; i <= ed; i++)
+            OFN(upd_lower_)(a, c, rhs, i - u, i, &aa[i - st], &cc[i - st],
+                            &rr[i - st]);
+        for (int i = st; i <= ed; i++) {
+            a[i] = aa[i - st];
+            c[i] = cc[i - st];
+            rhs[i] = rr[i - st];
+        }
+    }
+    int j = st / s;
+    ba[j] = a[st];
+    bc[j] = c[st];
+    br[j] = rhs[st];
+    OFN(est_update_)(a, c, rhs, st, ed);
+}
+
+/* Stage 3 of one slice: restore E_st, then every x of the slice from
+ * x[st - 1] and key = x[ed + 1] (src/ptpr.cpp:263-287). */
+static void OFN(ptpr_st3_slice_)(int s, int st, REAL *a, REAL *c, REAL *rhs,
+                                 const REAL *ba, const REAL *bc,
+                                 const REAL *br, REAL *xx) {
+    int j = st / s, ed = st + s - 1;
+    a[st] = ba[j];
+    c[st] = bc[j];
+    rhs[st] = br[j];
+    REAL key = ONE / c[ed] * (rhs[ed] - a[ed] * xx[st - 1] - xx[ed]);
+    if (c[ed] == (REAL)0) key = (REAL)0;
+    for (int i = st; i < ed; i++)
+        xx[i] = rhs[i] - a[i] * xx[st - 1] - c[i] * key;
+}
+
+/* PTPR driver.  nthreads <= 1: the slices one after the other, one s-sized
+ * stage-1 scratch.  nthreads > 1: stage 1 and stage 3 parallel over the
+ * slices, schedule(static), as the reference's solver-internal OpenMP does
+ * (src/ptpr.cpp:131, :264); each slice then has its own s-sized scratch
+ * block (scr, n elements).  The slices are independent in both stages, so
+ * both forms give the same bits. */
+static int OFN(ptpr_run_)(int n, int s, REAL *a, REAL *c, REAL *rhs, REAL *x,
+                          REAL *ws, REAL *scr, int nthreads) {
     int m = n / s;
     int ls = orc_ilog2(s), lm = orc_ilog2(m);
     REAL *aa = ws, *cc = ws + s, *rr = ws + 2 * s;
@@ -223,48 +281,30 @@ int OFN(orc_ptpr_ws_)(int n, int s, REAL *a, REAL *c, REAL *rhs, REAL *x,
     REAL *xx = xs + 1; /* xx[-1] == 0 sentinel, src/ptpr.cpp:66-70 */
     for (int i = 0; i < n + 1; i++) xs[i] = (REAL)0;
 
-    /* stage 1: PCR inside every slice, src/ptpr.cpp:130-213 */
-    for (int st = 0; st < n; st += s) {
-        int ed = st + s - 1;
-        for (int p = 1; p <= ls; p++) {
-            int u = 1 << (p - 1);
-            for (int i = st; i <= ed; i++) {
-                int li = i - st;
-                REAL *oa = &aa[li], *oc = &cc[li], *orr = &rr[li];
-                if (i < st + u)
-                    OFN(upd_upper_)(a, c, rhs, i, i + u, oa, oc, orr);
-                else if (i <= ed - u)
-                    OFN(upd_mid_)(a, c, rhs, i - u, i, i + u, oa, oc, orr);
-                else
-                    OFN(upd_lower_)(a, c, rhs, i - u, i, oa, oc, orr);
-            }
-            for (int i = st; i <= ed; i++) {
-                a[i] = aa[i - st];
-                c[i] = cc[i - st];
-                rhs[i] = rr[i - st];
-            }
-        }
-        int j = st / s;
-        ba[j] = a[st];
-        bc[j] = c[st];
-        br[j] = rhs[st];
-        OFN(est_update_)(a, c, rhs, st, ed);
+    /* stage 1: PCR inside every slice */
+    if (nthreads > 1) {
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+        for (int st = 0; st < n; st += s)
+            OFN(ptpr_st1_slice_)(s, ls, st, a, c, rhs, scr + st,
+                                 scr + n + st, scr + 2 * n + st, ba, bc, br);
+    } else {
+        for (int st = 0; st < n; st += s)
+            OFN(ptpr_st1_slice_)(s, ls, st, a, c, rhs, aa, cc, rr, ba, bc,
+                                 br);
     }
     /* intermediate + stage 2 (PCR on the m-system), src/ptpr.cpp:218-258 */
     OFN(tpr_inter_)(n, s, a, c, rhs, sa, sc, sr);
     OFN(orc_pcr_ws_)(m, sa, sc, sr, pws);
     for (int i = s - 1; i < n; i += s) xx[i] = sr[i / s];
 
-    /* stage 3, src/ptpr.cpp:263-287 */
-    for (int st = 0; st < n; st += s) {
-        int j = st / s, ed = st + s - 1;
-        a[st] = ba[j];
-        c[st] = bc[j];
-        rhs[st] = br[j];
-        REAL key = ONE / c[ed] * (rhs[ed] - a[ed] * xx[st - 1] - xx[ed]);
-        if (c[ed] == (REAL)0) key = (REAL)0;
-        for (int i = st; i < ed; i++)
-            xx[i] = rhs[i] - a[i] * xx[st - 1] - c[i] * key;
+    /* stage 3 */
+    if (nthreads > 1) {
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+        for (int st = 0; st < n; st += s)
+            OFN(ptpr_st3_slice_)(s, st, a, c, rhs, ba, bc, br, xx);
+    } else {
+        for (int st = 0; st < n; st += s)
+            OFN(ptpr_st3_slice_)(s, st, a, c, rhs, ba, bc, br, xx);
     }
     for (int i = 0; i < n; i++) x[i] = xx[i];
 
@@ -272,6 +312,11 @@ int OFN(orc_ptpr_ws_)(int n, int s, REAL *a, REAL *c, REAL *rhs, REAL *x,
     int fp2 = 9 * (m - 1) + (14 * m * lm);
     int fp3 = m * 4 * (s - 1);
     return fp1 + fp2 + fp3;
+}
+
+int OFN(orc_ptpr_ws_)(int n, int s, REAL *a, REAL *c, REAL *rhs, REAL *x,
+                      REAL *ws) {
+    return OFN(ptpr_run_)(n, s, a, c, rhs, x, ws, NULL, 1);
 }
 
 int OFN(orc_ptpr_)(int n, int s, REAL *a, REAL *c, REAL *rhs, REAL *x) {
@@ -290,8 +335,65 @@ size_t OFN(orc_tpr_ws_size_)(int n, int s) {
     return (size_t)(6 * n + 7 * m);
 }
 
-int OFN(orc_tpr_ws_)(int n, int s, REAL *a, REAL *c, REAL *rhs, REAL *x,
-                     REAL *ws) {
+/* Stage 1 of one slice [st, st + s): even-row backups, the tree levels
+ * (only rows i % 2^p == 0 and (i+1) % 2^p == 0 of the slice change), odd-row
+ * backups, the E_st update (src/tpr.cpp:123-230).  aa/cc/rr: n-sized
+ * scratch indexed by the row. */
+static void OFN(tpr_st1_slice_)(int s, int ls, int st, REAL *a, REAL *c,
+                                REAL *rhs, REAL *bka, REAL *bkc, REAL *bkr,
+                                REAL *aa, REAL *cc, REAL *rr) {
+    int ed = st + s - 1;
+    for (int i = st; i <= ed; i += 2) {
+        bka[i] = a[i];
+        bkc[i] = c[i];
+        bkr[i] = rhs[i];
+    }
+    for (int p = 1; p <= ls; p++) {
+        int u = 1 << (p - 1), p2k = 1 << p;
+        OFN(upd_upper_)(a, c, rhs, st, st + u, &aa[st], &cc[st], &rr[st]);
+        for (int i = st + p2k; i <= ed - u; i += p2k)
+            OFN(upd_mid_)(a, c, rhs, i - u, i, i + u, &aa[i], &cc[i], &rr[i]);
+        for (int i = st + p2k - 1; i <= ed - u; i += p2k)
+            OFN(upd_mid_)(a, c, rhs, i - u, i, i + u, &aa[i], &cc[i], &rr[i]);
+        OFN(upd_lower_)(a, c, rhs, ed - u, ed, &aa[ed], &cc[ed], &rr[ed]);
+        for (int i = st; i <= ed; i += p2k) {
+            a[i] = aa[i];
+            c[i] = cc[i];
+            rhs[i] = rr[i];
+        }
+        for (int i = st + p2k - 1; i <= ed; i += p2k) {
+            a[i] = aa[i];
+            c[i] = cc[i];
+            rhs[i] = rr[i];
+        }
+    }
+    for (int i = st + 1; i <= ed; i += 2) {
+        bka[i] = a[i];
+        bkc[i] = c[i];
+        bkr[i] = rhs[i];
+    }
+    OFN(est_update_)(a, c, rhs, st, ed);
+}
+
+/* Stage 3 of one slice: log2(s) back-substitution levels from the slice's
+ * last x and x[st - 1] (src/tpr.cpp:277-308). */
+static void OFN(tpr_st3_slice_)(int s, int ls, int st, const REAL *a,
+                                const REAL *c, const REAL *rhs, REAL *x) {
+    int ed = st + s - 1;
+    for (int p = ls - 1; p >= 0; p--) {
+        int u = 1 << p;
+        int i = st + u - 1;
+        REAL xu = (i - u < 0) ? (REAL)0 : x[i - u];
+        x[i] = rhs[i] - a[i] * xu - c[i] * x[i + u];
+        for (i = st + u - 1 + 2 * u; i <= ed; i += 2 * u)
+            x[i] = rhs[i] - a[i] * x[i - u] - c[i] * x[i + u];
+    }
+}
+
+/* TPR driver; nthreads > 1 runs stages 1 and 3 parallel over the slices as
+ * the reference does (src/tpr.cpp:124, :278) -- same bits as one thread. */
+static int OFN(tpr_run_)(int n, int s, REAL *a, REAL *c, REAL *rhs, REAL *x,
+                         REAL *ws, int nthreads) {
     int m = n / s;
     int ls = orc_ilog2(s);
     REAL *bka = ws, *bkc = ws + n, *bkr = ws + 2 * n;
@@ -299,70 +401,36 @@ int OFN(orc_tpr_ws_)(int n, int s, REAL *a, REAL *c, REAL *rhs, REAL *x,
     REAL *st2 = ws + 6 * n;
     REAL *sa = st2, *sc = st2 + m, *sr = st2 + 2 * m, *sx = st2 + 3 * m;
     REAL *cws = st2 + 4 * m; /* 3m for the stage-2 CR */
+    int nt = nthreads > 1 ? nthreads : 1;
 
-    /* stage 1, src/tpr.cpp:123-230 */
-    for (int st = 0; st < n; st += s) {
-        int ed = st + s - 1;
-        for (int i = st; i <= ed; i += 2) {
-            bka[i] = a[i];
-            bkc[i] = c[i];
-            bkr[i] = rhs[i];
-        }
-        for (int p = 1; p <= ls; p++) {
-            int u = 1 << (p - 1), p2k = 1 << p;
-            OFN(upd_upper_)(a, c, rhs, st, st + u, &aa[st], &cc[st], &rr[st]);
-            for (int i = st + p2k; i <= ed - u; i += p2k)
-                OFN(upd_mid_)(a, c, rhs, i - u, i, i + u, &aa[i], &cc[i],
-                              &rr[i]);
-            for (int i = st + p2k - 1; i <= ed - u; i += p2k)
-                OFN(upd_mid_)(a, c, rhs, i - u, i, i + u, &aa[i], &cc[i],
-                              &rr[i]);
-            OFN(upd_lower_)(a, c, rhs, ed - u, ed, &aa[ed], &cc[ed], &rr[ed]);
-            for (int i = st; i <= ed; i += p2k) {
-                a[i] = aa[i];
-                c[i] = cc[i];
-                rhs[i] = rr[i];
-            }
-            for (int i = st + p2k - 1; i <= ed; i += p2k) {
-                a[i] = aa[i];
-                c[i] = cc[i];
-                rhs[i] = rr[i];
-            }
-        }
-        for (int i = st + 1; i <= ed; i += 2) {
-            bka[i] = a[i];
-            bkc[i] = c[i];
-            bkr[i] = rhs[i];
-        }
-        OFN(est_update_)(a, c, rhs, st, ed);
-    }
+    /* stage 1 */
+#pragma omp parallel for schedule(static) num_threads(nt) if (nt > 1)
+    for (int st = 0; st < n; st += s)
+        OFN(tpr_st1_slice_)(s, ls, st, a, c, rhs, bka, bkc, bkr, aa, cc, rr);
     /* intermediate + stage 2 (CR on the m-system), src/tpr.cpp:235-275 */
     OFN(tpr_inter_)(n, s, a, c, rhs, sa, sc, sr);
     OFN(orc_cr_ws_)(m, sa, sc, sr, sx, cws);
     for (int i = 0; i < m; i++) x[(i + 1) * s - 1] = sx[i];
 
-    /* stage 3: restore backups then log2(s) back-substitution levels,
-     * src/tpr.cpp:277-308, 381-387 */
+    /* stage 3: restore backups (src/tpr.cpp:381-387), then back
+     * substitution per slice */
     for (int i = 0; i < n; i++) {
         a[i] = bka[i];
         c[i] = bkc[i];
         rhs[i] = bkr[i];
     }
-    for (int st = 0; st < n; st += s) {
-        int ed = st + s - 1;
-        for (int p = ls - 1; p >= 0; p--) {
-            int u = 1 << p;
-            int i = st + u - 1;
-            REAL xu = (i - u < 0) ? (REAL)0 : x[i - u];
-            x[i] = rhs[i] - a[i] * xu - c[i] * x[i + u];
-            for (i = st + u - 1 + 2 * u; i <= ed; i += 2 * u)
-                x[i] = rhs[i] - a[i] * x[i - u] - c[i] * x[i + u];
-        }
-    }
+#pragma omp parallel for schedule(static) num_threads(nt) if (nt > 1)
+    for (int st = 0; st < n; st += s)
+        OFN(tpr_st3_slice_)(s, ls, st, a, c, rhs, x);
     int fp1 = 28 * n - 14 * m;
     int fp2 = 9 * (m - 1) + 17 * m;
     int fp3 = m * 4 * (s - 1);
     return fp1 + fp2 + fp3;
+}
+
+int OFN(orc_tpr_ws_)(int n, int s, REAL *a, REAL *c, REAL *rhs, REAL *x,
+                     REAL *ws) {
+    return OFN(tpr_run_)(n, s, a, c, rhs, x, ws, 1);
 }
 
 int OFN(orc_tpr_)(int n, int s, REAL *a, REAL *c, REAL *rhs, REAL *x) {
@@ -370,6 +438,43 @@ int OFN(orc_tpr_)(int n, int s, REAL *a, REAL *c, REAL *rhs, REAL *x) {
     int r = OFN(orc_tpr_ws_)(n, s, a, c, rhs, x, ws);
     free(ws);
     return r;
+}
+
+/* ------------------------------------------------------------------------
+ * The reference's timed plain-solve loop (src/pm.cpp:160-194): one solver
+ * object (workspace allocated once, as its init does), then per iteration
+ * the system is assigned afresh (untimed: the solve overwrites a, c, rhs)
+ * and solve() + get_ans() are timed.  kind 0 = PTPR, 1 = TPR; nthreads > 1
+ * runs the solver-internal OpenMP of stages 1 and 3.  a, c, rhs are the
+ * diag-normalised system (the 3-argument setter, as tpr_pm uses).  Returns
+ * the seconds spent in solve + get_ans over all iterations; x receives the
+ * last solution.
+ * ---------------------------------------------------------------------- */
+double OFN(orc_time_plain_)(int kind, int n, int s, const REAL *a,
+                            const REAL *c, const REAL *rhs, int iters,
+                            int nthreads, REAL *x) {
+    size_t wsz = kind == 0 ? OFN(orc_ptpr_ws_size_)(n, s)
+                           : OFN(orc_tpr_ws_size_)(n, s);
+    REAL *ws = (REAL *)malloc(sizeof(REAL) * (wsz + 3 * (size_t)n));
+    REAL *scr = ws + wsz;
+    REAL *wa = (REAL *)malloc(sizeof(REAL) * 4 * (size_t)n);
+    REAL *wc = wa + n, *wr = wa + 2 * n, *xo = wa + 3 * n;
+    double total = 0.0;
+    for (int it = 0; it < iters; it++) {
+        memcpy(wa, a, sizeof(REAL) * (size_t)n);
+        memcpy(wc, c, sizeof(REAL) * (size_t)n);
+        memcpy(wr, rhs, sizeof(REAL) * (size_t)n);
+        double t0 = orc_now();
+        if (kind == 0)
+            OFN(ptpr_run_)(n, s, wa, wc, wr, xo, ws, scr, nthreads);
+        else
+            OFN(tpr_run_)(n, s, wa, wc, wr, xo, ws, nthreads);
+        memcpy(x, xo, sizeof(REAL) * (size_t)n); /* get_ans */
+        total += orc_now() - t0;
+    }
+    free(wa);
+    free(ws);
+    return total;
 }
 
 #undef OFN

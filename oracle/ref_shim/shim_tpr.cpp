@@ -39,3 +39,28 @@ extern "C" void ref_batch_tpr(int nsys, int n, int s, const real *a,
         }
     }
 }
+
+// The timed plain-solve loop of tpr_pm (src/pm.cpp:160-194): one solver,
+// per iteration a fresh copy of the diag-normalised system (untimed: the
+// solve overwrites it), the 3-argument setter, then solve() + get_ans()
+// timed, with the solver's own OpenMP on nthreads threads.  Returns the
+// seconds spent in solve + get_ans; x receives the last solution.
+extern "C" double ref_time_plain_tpr(int n, int s, const real *a, const real *c,
+                                    const real *rhs, int iters, int nthreads,
+                                    real *x) {
+    omp_set_num_threads(nthreads > 0 ? nthreads : 1);
+    TPR t(n, s);
+    std::vector<real> wa(n), wc(n), wr(n);
+    double total = 0.0;
+    for (int it = 0; it < iters; it++) {
+        std::memcpy(wa.data(), a, sizeof(real) * n);
+        std::memcpy(wc.data(), c, sizeof(real) * n);
+        std::memcpy(wr.data(), rhs, sizeof(real) * n);
+        t.set_tridiagonal_system(wa.data(), wc.data(), wr.data());
+        double t0 = omp_get_wtime();
+        t.solve();
+        t.get_ans(x);
+        total += omp_get_wtime() - t0;
+    }
+    return total;
+}

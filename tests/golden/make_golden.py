@@ -1,8 +1,9 @@
 """Regenerate the golden fixtures in this directory.
 
-Run in a container that holds the reference tree at /root/reference:
+Run where the reference tree is present: TPR_REFERENCE_ROOT names it
+(default: a `reference` directory beside this repository's root):
 
-    python tests/golden/make_golden.py
+    TPR_REFERENCE_ROOT=<reference tree> python tests/golden/make_golden.py
 
 It writes
   ans1024.npy      the reference's known answer test/ans1024.txt (solution
@@ -34,7 +35,7 @@ sys.path.insert(0, ROOT)
 from oracle import oracle as O  # noqa: E402
 from tpr_gb300 import generate as G  # noqa: E402
 
-REF = "/root/reference"
+REF = O.REFERENCE_ROOT
 
 
 def read_ans1024() -> np.ndarray:

@@ -138,3 +138,33 @@ def test_reference_build_agrees_when_present(port):
                                       r.ptpr(an, cn, rn, s)[0])
         np.testing.assert_array_equal(port.tpr(an, cn, rn, s)[0],
                                       r.tpr(an, cn, rn, s)[0])
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_timed_plain_loop_threads_same_bits(port, golden, prec):
+    """The timed single-system loop with solver-internal OpenMP (stages 1
+    and 3 parallel over slices) gives the fixtures' bits at any thread
+    count, so the timed CPU baseline computes what the reference computes."""
+    dt = np.float32 if prec == "f32" else np.float64
+    a, b, c, d, _ = G.one_system(2048, 42, "dominant")
+    an, cn, rn = port.normalize(a, b, c, d, dt)
+    for kind, name in ((0, "ptpr"), (1, "tpr")):
+        for threads in (1, 3, 4):
+            t, x = port.time_plain(kind, an, cn, rn, 512, 3, threads, dt)
+            assert t > 0.0
+            np.testing.assert_array_equal(x, golden[f"plain_{name}_s512_{prec}"])
+
+
+def test_reference_timed_loop_agrees_when_present(port):
+    """Where the reference was compiled here, its own timed loop (the
+    tpr_pm pattern) returns the port's bits."""
+    from oracle import oracle as O
+    r = O.ref("f32")
+    if r is None:
+        pytest.skip("reference solvers not built on this machine")
+    a, b, c, d, _ = G.one_system(2048, 42, "dominant")
+    an, cn, rn = port.normalize(a, b, c, d)
+    for kind in (0, 1):
+        _, xr = r.time_plain(kind, an, cn, rn, 512, 3, 4)
+        _, xp = port.time_plain(kind, an, cn, rn, 512, 3, 4)
+        np.testing.assert_array_equal(xp, xr)
