@@ -88,14 +88,16 @@ TPRGB_API int tprgb_ref_solve_device(int kind, int nsys, int n, int s,
                                      void *d_x, void *d_work,
                                      size_t work_bytes, void *stream);
 
-/* Same as tprgb_ref_solve_device, but allocation-free: the workspace is the
- * library's own 16 MiB device array, for callers that cannot call
- * cudaMalloc (inside stream capture, in latency-critical loops, or under a
- * host framework that owns device memory).  No counterpart in the
- * reference.  The first call on a device looks up the array's address, so
- * make it before any stream capture; workspace needs above 16 MiB
- * (nsys * (3n + 3n/s) elements) return TPRGB_EUNSUPPORTED; all calls share
- * the array, so calls that overlap on the GPU race. */
+/* Same as tprgb_ref_solve_device, but allocation-free, for callers that
+ * cannot call cudaMalloc: plugins whose device memory belongs to a host
+ * framework's allocator, and latency-critical loops where an allocation
+ * would synchronise the device.  No counterpart in the reference.  The
+ * workspace is the library's own 16 MiB device array (held by every GPU
+ * that loads the library until exit).  The first call on a device (and
+ * after a cudaDeviceReset) looks up the array's address, so make it before
+ * any stream capture; workspace needs above 16 MiB (nsys * (3n + 3n/s)
+ * elements) return TPRGB_EUNSUPPORTED; all calls share the array, so calls
+ * that overlap on the GPU race. */
 TPRGB_API int tprgb_ref_solve_device_static(int kind, int nsys, int n, int s,
                                             int prec, const void *d_a,
                                             const void *d_c, const void *d_rhs,

@@ -92,7 +92,7 @@ __device__ void ptpr_stage1(T *a, T *c, T *r, int n, int s) {
     }
 }
 
-// TPR stage 1 tree levels (src/tpr.cpp:246-317): at level p only rows with
+// TPR stage 1 tree levels (src/tpr.cpp:123-230): at level p only rows with
 // li % 2^p == 0 or (li+1) % 2^p == 0 are updated.
 template <typename T>
 __device__ void tpr_stage1(T *a, T *c, T *r, int n, int s) {
@@ -732,14 +732,16 @@ int launch_normalize(int prec, long long neq, void *a, const void *diag,
 }  // namespace tprgb
 
 // ---- reference-semantics solve with a built-in workspace ---------------------
-// For callers that cannot allocate device memory: code running inside CUDA
-// stream capture (a cudaMalloc there is not captured and may synchronise),
-// latency-critical loops where an allocation would stall the device, and
-// host applications or plugins whose device memory is owned by another
-// allocator that forbids outside allocations.  The sliced path's workspace
+// For callers that cannot allocate device memory themselves: plugins and
+// host applications whose device memory belongs to another allocator (a
+// framework's caching pool, a simulation code's own arena) that forbids or
+// cannot see outside cudaMalloc calls, and latency-critical loops where an
+// allocation would synchronise the device.  The sliced path's workspace
 // (3n + 3n/s elements per system) lives in this file-scope array instead of
-// caller memory.  Every GPU that loads the library reserves it until the
+// caller memory.  Every GPU that loads the library holds it until the
 // process exits.
+#include <cuda.h>  // CUcontext (driver entry points fetched at run time)
+
 #include <mutex>
 
 namespace tprgb {
@@ -747,23 +749,69 @@ namespace tprgb {
 constexpr size_t kStaticWorkBytes = 16u << 20;  // 16 MiB
 static __device__ __align__(256) unsigned char g_static_work[kStaticWorkBytes];
 
-// Device address of g_static_work per device, looked up once per device
-// (with that device current) on the first call made on it.
+// The array's device address belongs to the context the library's module
+// is loaded in.  It is looked up (cudaGetSymbolAddress, with the device
+// current) once per device and context: a cudaDeviceReset, or a caller that
+// makes another driver context current, gives a new context id and hence
+// a new lookup, never a stale address.
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+
+static int current_ctx_id(unsigned long long *id) {
+    static std::atomic<CtxGetCurrentFn> get_cur{nullptr};
+    static std::atomic<CtxGetIdFn> get_id{nullptr};
+    CtxGetCurrentFn f1 = get_cur.load(std::memory_order_acquire);
+    CtxGetIdFn f2 = get_id.load(std::memory_order_acquire);
+    if (!f1 || !f2) {
+        void *p1 = nullptr, *p2 = nullptr;
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+        cudaError_t e1 = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p1, 12000,
+                                                          cudaEnableDefault, &q1);
+        cudaError_t e2 = cudaGetDriverEntryPointByVersion("cuCtxGetId", &p2, 12000,
+                                                          cudaEnableDefault, &q2);
+        if (e1 != cudaSuccess || e2 != cudaSuccess || q1 != cudaDriverEntryPointSuccess ||
+            q2 != cudaDriverEntryPointSuccess || !p1 || !p2)
+            return fail(TPRGB_EUNSUPPORTED, "cuCtxGetCurrent / cuCtxGetId not available");
+        f1 = reinterpret_cast<CtxGetCurrentFn>(p1);
+        f2 = reinterpret_cast<CtxGetIdFn>(p2);
+        get_cur.store(f1, std::memory_order_release);
+        get_id.store(f2, std::memory_order_release);
+    }
+    CUcontext ctx = nullptr;
+    if (f1(&ctx) != CUDA_SUCCESS) return fail(TPRGB_ECUDA, "cuCtxGetCurrent failed");
+    *id = 0;  // 0: no context current yet on this thread
+    if (ctx && f2(ctx, id) != CUDA_SUCCESS) return fail(TPRGB_ECUDA, "cuCtxGetId failed");
+    return TPRGB_OK;
+}
+
+struct StaticSlot {
+    unsigned long long ctx_id;  // context the address belongs to (0: none)
+    void *ptr;
+};
 static std::mutex g_static_mu;
-static void *g_static_ptr[64];
+static StaticSlot g_static_slot[64];
 
 static int static_work_ptr(void **out) {
     int dev = 0;
     TPRGB_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) return fail(TPRGB_EUNSUPPORTED, "device %d", dev);
+    unsigned long long id = 0;
+    int rc = current_ctx_id(&id);
+    if (rc) return rc;
     std::lock_guard<std::mutex> lk(g_static_mu);
-    if (!g_static_ptr[dev]) {
+    StaticSlot &sl = g_static_slot[dev];
+    if (id == 0 || sl.ctx_id != id || !sl.ptr) {
+        // set-up for this device and context: the runtime makes the
+        // device's context current first if none is
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_static_work);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_static_work)");
-        g_static_ptr[dev] = p;
+        rc = current_ctx_id(&id);
+        if (rc) return rc;
+        sl.ctx_id = id;
+        sl.ptr = p;
     }
-    *out = g_static_ptr[dev];
+    *out = sl.ptr;
     return TPRGB_OK;
 }
 
@@ -771,14 +819,16 @@ static int static_work_ptr(void **out) {
 
 // Same contract and results as tprgb_ref_solve_device, with the workspace
 // taken from the library's own 16 MiB device array instead of the caller:
-// nothing is allocated.  The first call on a device looks up the array's
-// device address (cudaGetSymbolAddress), so make that first call before any
-// stream capture.  Systems whose workspace exceeds 16 MiB in total
-// (nsys * (3n + 3n/s) elements) are rejected with TPRGB_EUNSUPPORTED.
-// All calls share the array (no part of it needs to start at zero: every
-// workspace element is written before it is read), so calls that overlap on
-// the GPU -- on different streams, or from different threads -- race; keep
-// them ordered on one stream.
+// nothing is allocated (no cudaMalloc, no cudaFree, no allocating library
+// call).  The first call on a device (and after a cudaDeviceReset, or under
+// another driver context) looks up the array's device address with
+// cudaGetSymbolAddress; make that first call before any stream capture.
+// Systems whose workspace exceeds 16 MiB in total (nsys * (3n + 3n/s)
+// elements) are rejected with TPRGB_EUNSUPPORTED.  All calls share the
+// array and it keeps the last call's contents (no part of it needs to
+// start at zero: every workspace element is written before it is read), so
+// calls that overlap on the GPU -- on different streams, or from different
+// threads -- race; keep them ordered on one stream.
 extern "C" TPRGB_API int tprgb_ref_solve_device_static(
     int kind, int nsys, int n, int s, int prec, const void *d_a,
     const void *d_c, const void *d_rhs, void *d_x, void *stream) {
