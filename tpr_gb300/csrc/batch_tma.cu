@@ -81,10 +81,15 @@ batch_tma(const float *__restrict__ ga, const float *__restrict__ gb,
         }
         __syncthreads();
         if (!s_ok) {
-            // drain the other stage's copies (bounded) before leaving
-            if (tid == 0 && tl + stride < ntiles)
-                tma::mbar_wait(&full[st ^ 1], (unsigned)((it + 1) >> 1) & 1u,
-                               kWaitLimit);
+            // leave no copy in flight: thread 0 waits (bounded again) for
+            // the late copies into the stage that timed out, then for the
+            // other stage's copies if they were issued
+            if (tid == 0) {
+                tma::mbar_wait(&full[st], phase, kWaitLimit);
+                if (tl + stride < ntiles)
+                    tma::mbar_wait(&full[st ^ 1], (unsigned)((it + 1) >> 1) & 1u,
+                                   kWaitLimit);
+            }
             return;
         }
         const int g = tid / T, t = tid & (T - 1);
