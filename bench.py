@@ -14,8 +14,12 @@ collective on the data path (the systems are independent).
 
 --impl reference times the reference algorithm's CPU implementation (PTPR,
 FP32, OpenMP over systems, all host threads) on a bounded sample of the same
-workload per step: the reference's own solvers compiled from its sources
-where present (oracle/_ref), else the C restatement (oracle port).
+workload per step (2048 systems, more when few steps are asked for, so that
+the timed steps take about a second): the reference's own solvers compiled
+from its sources where present (oracle/_ref), else the C restatement (oracle
+port, same bits).  The in-arm cpu_baseline times the same 2048-system
+samples for --cpu-seconds; plain_single_system adds the N=2048, S=512 single
+solve on the GPU beside the reference's CPU PTPR / TPR on the host cores.
 """
 from __future__ import annotations
 
@@ -37,7 +41,16 @@ NSYS, N, SLICE = 16384, 1024, 128
 REFINE = 1
 ALGO_BYTES_PER_EQ = 16 + 8  # a, b, c, d FP32 in + x FP64 out
 METRIC = "systems/s"
-WORKLOAD = "uniform batch 16384 x N=1024 (S=128), FP32 + 1 refinement step"
+# The workload both arms solve (identical in both lines); how each arm
+# solves it goes under "solver".
+CONFIG = {
+    "workload": "uniform ADI batch: 16384 independent tridiagonal systems "
+                "x N=1024, FP32 a, b, c, d (a,c~U(-1,1), b=|a|+|c|+U(1,2), "
+                "d=A x_t), seeded",
+    "nsys_per_gpu": NSYS, "n": N,
+    "l2": "inputs 268 MB > 129 MB L2 (no flush needed)",
+}
+CPU_SAMPLE = 2048  # systems per CPU step (both CPU legs)
 
 
 def env_rank():
@@ -142,7 +155,8 @@ def profiled_traffic():
 
 def cpu_reference_sample(port_or_ref, bt, nsys_sample, threads):
     """One bounded CPU step: PTPR FP32 (4-arg setter inside) over
-    nsys_sample systems; returns seconds."""
+    nsys_sample systems, OpenMP over systems with one solver object per
+    thread; returns seconds."""
     n = N
     sl = slice(0, nsys_sample * n)
     a, b, c, d = (np.ascontiguousarray(v[sl]) for v in
@@ -163,6 +177,53 @@ def cpu_impl():
     return O.port(), "port"
 
 
+def cpu_solver(kind, sample, threads):
+    return {"kind": f"reference PTPR, FP32, no refinement ({kind})",
+            "s": SLICE, "sample_systems_per_step": sample,
+            "threads": threads,
+            "parallelism": "OpenMP over systems, one solver object per "
+                           "thread (the reference's multi-thread test)"}
+
+
+def cpu_sample_size(rate, steps):
+    """Systems per CPU step: CPU_SAMPLE, raised (in CPU_SAMPLE multiples,
+    up to the whole batch) so that the timed steps together take about a
+    second at the measured rate."""
+    want = rate * 1.0 / max(1, steps)
+    k = max(1, min(NSYS // CPU_SAMPLE, int(np.ceil(want / CPU_SAMPLE))))
+    return k * CPU_SAMPLE
+
+
+def plain_row(iters=1000):
+    """The plain single-system configuration (N=2048, S=512, FP32, seed
+    42): the GPU class path (host arrays in and out, as the reference's
+    timed loop, src/pm.cpp:160-194, and the device-only kernel time) beside
+    the reference's CPU PTPR / TPR timed the same way on this machine's host
+    cores with their solver-internal OpenMP (one thread and all cores)."""
+    from tpr_gb300 import workloads as W
+    from tpr_gb300 import generate as G
+    gpu = W.plain(iters)
+    impl, kind = cpu_impl()
+    from oracle import oracle as O
+    port = O.port()
+    a, b, c, d, xt = G.one_system(2048, 42, "dominant")
+    an, cn, rn = port.normalize(a, b, c, d)
+    cores = os.cpu_count() or 1
+    cpu = {"kind": kind, "cores": cores, "iters": iters}
+    for kid, name in ((0, "ptpr"), (1, "tpr")):
+        res = {}
+        for threads in sorted({1, cores}):
+            impl.time_plain(kid, an, cn, rn, 512, 10, threads)  # warm-up
+            t, x = impl.time_plain(kid, an, cn, rn, 512, iters, threads)
+            res[f"us_per_solve_{threads}t"] = t * 1e6 / iters
+            res["rel_l2_vs_xt"] = float(
+                np.linalg.norm(x.astype(np.float64) - xt) / np.linalg.norm(xt))
+        cpu[name] = res
+    gpu.pop("workload", None)
+    return {"workload": "one system N=2048, S=512, FP32, seed 42, "
+                        f"{iters} solves", "gpu": gpu, "cpu_reference": cpu}
+
+
 def run_reference(args):
     rank, world, _ = env_rank()
     if rank != 0:
@@ -170,8 +231,9 @@ def run_reference(args):
     from tpr_gb300 import generate as G
     impl, kind = cpu_impl()
     threads = os.cpu_count() or 1
-    sample = 512
-    bt = G.uniform_batch(sample, N, 12345, "dominant")
+    bt = G.uniform_batch(NSYS, N, 1_000_000, "dominant")
+    t = cpu_reference_sample(impl, bt, CPU_SAMPLE, threads)
+    sample = cpu_sample_size(CPU_SAMPLE / t, args.steps)
     for _ in range(args.warmup):
         cpu_reference_sample(impl, bt, sample, threads)
     times = [cpu_reference_sample(impl, bt, sample, threads)
@@ -184,17 +246,42 @@ def run_reference(args):
         "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded generator, dominant)",
-        "config": {"workload": WORKLOAD, "nsys": NSYS, "n": N, "s": SLICE,
-                   "sample_systems_per_step": sample, "solver": "PTPR"},
+        "config": dict(CONFIG),
+        "solver": cpu_solver(kind, sample, threads),
         "cpu_baseline": {"value": value, "unit": "systems/s",
                          "cores": threads, "kind": kind,
                          "sample": f"{sample} systems x N={N}, S={SLICE} "
-                                   f"per step, OpenMP over systems"},
+                                   f"per step, {args.steps} steps, OpenMP "
+                                   f"over systems"},
         "e2e": {"value": value, "unit": "systems/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def solver_desc(B, n, tuned, world):
+    """How this arm solves the workload: the kernel's tile and what plays
+    the reference's slice.  The hierarchical solver has no slice size S:
+    a thread reduces its chunk of L equations, a warp segment of 32 lanes
+    (32 L equations, the in-slice reduction) and the warps of a system
+    (the inter-slice system) in turn."""
+    L, nt, variant = B.tile_for(n)
+    tps = min(nt, n // L)  # threads per system
+    return {"kind": "hierarchical TPR, FP32 + 1 refinement step with a "
+                    "compensated FP32 (double-float) residual",
+            "refine_steps": REFINE, "residual": "compensated FP32",
+            "x": "FP64",
+            "tile": {"eq_per_thread": L, "threads_per_cta": nt,
+                     "variant": variant, "threads_per_system": tps,
+                     "systems_per_cta": max(1, nt // tps)},
+            "levels_eq": {"thread_chunk": L,
+                          "warp_segment": L * min(32, tps),
+                          "system": n},
+            "tuned_entries": tuned,
+            "parallelism": f"replicas x{world}",
+            "e2e_host_layout": "a, b, c, d in one pinned block, x pinned; "
+                               "chunks of 4 M equations"}
 
 
 def run_ours(args):
@@ -294,21 +381,22 @@ def run_ours(args):
     achieved = algo_bytes / (kernel_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
 
-    cpu = None
+    cpu = plain = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         impl, kind = cpu_impl()
         threads = os.cpu_count() or 1
-        sample = 2048
-        cpu_reference_sample(impl, bt, 256, threads)
+        sample = CPU_SAMPLE
+        cpu_reference_sample(impl, bt, sample, threads)
         reps, spent = 0, 0.0
         while spent < args.cpu_seconds:
             spent += cpu_reference_sample(impl, bt, sample, threads)
             reps += 1
         cpu = {"value": sample * reps / spent, "unit": "systems/s",
                "cores": threads, "kind": kind,
-               "sample": f"{reps} x {sample} systems of the same workload "
-                         f"(N={N}, S={SLICE}, PTPR FP32, no refinement), "
-                         f"OpenMP over systems"}
+               "sample": f"{reps} steps x {sample} systems of the same "
+                         f"workload (N={N}, S={SLICE}, PTPR FP32, no "
+                         f"refinement), OpenMP over systems"}
+        plain = plain_row()
 
     if rank == 0:
         line = {
@@ -318,16 +406,8 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generator: a,c~U(-1,1), "
                     "b=|a|+|c|+U(1,2), d=A x_t)",
-            "config": {"workload": WORKLOAD, "nsys_per_gpu": NSYS, "n": N,
-                       "s": SLICE, "refine_steps": REFINE,
-                       "residual": "compensated FP32",
-                       "tile": dict(zip(("eq_per_thread", "threads_per_cta",
-                                         "variant"), B.tile_for(N))),
-                       "tuned_entries": tuned,
-                       "x": "FP64", "parallelism": f"replicas x{world}",
-                       "l2": "inputs 268 MB > 129 MB L2 (no flush needed)",
-                       "e2e_host_layout": "a, b, c, d in one pinned block, "
-                                          "x pinned; chunks of 4 M equations"},
+            "config": dict(CONFIG),
+            "solver": solver_desc(B, N, tuned, world),
             "rel_l2_max": worst, "rel_l2_max_e2e": worst_e2e,
             "gb_per_s": achieved,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
@@ -343,6 +423,8 @@ def run_ours(args):
         }
         if cpu:
             line["cpu_baseline"] = cpu
+        if plain:
+            line["plain_single_system"] = plain
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -5,7 +5,8 @@
 plain       one system, N=2048, S=512, FP32 (seed 42): PTPR and TPR through
             the class surface (host arrays in and out, like the reference's
             timed loop, src/pm.cpp:178-194) and the device-only kernel time;
-            1000 solves.
+            1000 solves (bench.py's line carries the same numbers beside the
+            reference's CPU PTPR / TPR timed on the host cores).
 one_launch  the plain one-launch-per-system FP32 path (reference-semantics
             PTPR kernel launched once per system) on 16384 x N=1024, S=128,
             against the batched refined solver on the same systems.
