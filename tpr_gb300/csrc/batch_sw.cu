@@ -239,16 +239,17 @@ batch_sw(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
 // ---- systems spanning a thread-block cluster --------------------------------
 // One cluster of P CTAs per system of n = P * NT * L equations; CTA rank p
 // stages rows [p * ROWS, (p + 1) * ROWS) of the system's 128-byte rows with
-// a swizzled tensor-map load and solves its part; each solve's level 3 has
-// every part send its two boundary rows into every part's shared memory
-// (st.async onto a row mbarrier per parity, see tile::solve).  Clusters
+// a swizzled tensor-map load and solves its part; in each solve every warp
+// sends its segment's two boundary rows into every part's shared memory
+// (st.async onto a row mbarrier per parity) and warp 0 of each part solves
+// the system's reduced rows (tile::cluster_levels23).  Clusters
 // walk the batch with a stride of the number of clusters; every CTA of a
 // cluster runs the same number of systems and solves, so their row
 // exchanges pair up.  A load that times out is recorded in the status
 // word, its CTA stores nothing for that system, and the CTA keeps taking
 // part in the exchanges.  sys_off / sys_status / status as for batch_sw
 // (offsets multiples of 32).
-template <int L, int NT, int MODE>
+template <int L, int NT, int MODE, int P>
 __global__ void __launch_bounds__(NT, sw_min_blocks(L, NT))
 batch_cl(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
          int refine_steps, int x_f64, const long long *__restrict__ sys_off,
@@ -261,11 +262,11 @@ batch_cl(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
     float *stage = reinterpret_cast<float *>(dyn_sw + pad);  // [4][TILE]
     __shared__ __align__(8) uint64_t full;
     __shared__ tile::Smem<NT> sm;
-    __shared__ float4 crows[tile::kClusterRowSlots];
+    __shared__ float4 crows[tile::cluster_row_slots<NT, P>()];
     __shared__ __align__(8) uint64_t rbar[2];  // row barriers, one per parity
     __shared__ int s_ok;
     const int tid = threadIdx.x;
-    const unsigned P = cl::size(), p = cl::rank();
+    const unsigned p = cl::rank();  // the cluster has P CTAs
     const long long nclusters = gridDim.x / P, c0 = blockIdx.x / P;
     const long long rows_per_sys = (long long)P * ROWS;
     unsigned *stw = status ? status : g_sw_status;
@@ -323,7 +324,7 @@ batch_cl(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
         pc.crows = crows;
         pc.rbar = rbar;
         pc.cstatus = stw;
-        pc.P = (int)P;
+        pc.P = P;
         pc.p = (int)p;
         pc.round = round;
         pc.nsolve = 0;
@@ -334,7 +335,7 @@ batch_cl(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
             __syncthreads();  // every thread is done reading the stage
             if (tid == 0 && !pending && sys + nclusters < nsys) issue(sys + nclusters);
         };
-        const bool finite = tile::run_tile_smem<L, NT, NT, MODE, true>(
+        const bool finite = tile::run_tile_smem<L, NT, NT, MODE, true, decltype(early), P>(
             stage, stage + TILE, stage + 2 * TILE, stage + 3 * TILE, off, gx,
             ok ? base : 0, ok, tid, p == 0 && tid == 0,
             p == P - 1 && tid == NT - 1, refine_steps, x_f64, sm, pc, early);
@@ -520,13 +521,13 @@ int launch_batch_sw(const BatchArgs &A, const TileConfig &cfg, cudaStream_t st) 
 }
 
 // ---- cluster variant: host side ---------------------------------------------
-template <int L, int NT, int MODE>
-static int launch_cl_t(const BatchArgs &A, int P, cudaStream_t st) {
+template <int L, int NT, int MODE, int P>
+static int launch_cl_t(const BatchArgs &A, cudaStream_t st) {
     constexpr int TILE = NT * L;
     constexpr int ROWS = TILE / 32;
     const size_t smem = 4ull * TILE * sizeof(float) + 1024;
-    auto k = bt::batch_cl<L, NT, MODE>;
-    static DeviceOnce attrs, max_clusters[17];  // max_clusters by cluster size
+    auto k = bt::batch_cl<L, NT, MODE, P>;
+    static DeviceOnce attrs, max_clusters;
     int dev = 0;
     TPRGB_CUDA(cudaGetDevice(&dev));
     if (!attrs.get(dev)) {
@@ -547,13 +548,13 @@ static int launch_cl_t(const BatchArgs &A, int P, cudaStream_t st) {
     cfg.stream = st;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    int ncl_max = max_clusters[P].get(dev);
+    int ncl_max = max_clusters.get(dev);
     if (!ncl_max) {
         TPRGB_CUDA(cudaOccupancyMaxActiveClusters(&ncl_max, k, &cfg));
         if (ncl_max < 1)
             return fail(TPRGB_EUNSUPPORTED, "a cluster of %d CTAs of %d threads does not fit",
                         P, NT);
-        max_clusters[P].set(dev, ncl_max);
+        max_clusters.set(dev, ncl_max);
     }
     bt::TensorMaps tm;
     int rc = tile_maps(A, dev, (unsigned)ROWS, &tm);
@@ -565,10 +566,21 @@ static int launch_cl_t(const BatchArgs &A, int P, cudaStream_t st) {
     return TPRGB_OK;
 }
 
+template <int NT, int P>
+static int launch_cl_mode(const BatchArgs &A, cudaStream_t st) {
+    if (A.refine_steps <= 0) return launch_cl_t<16, NT, 0, P>(A, st);
+    return launch_cl_t<16, NT, 1, P>(A, st);
+}
+
 template <int NT>
-static int launch_cl_mode(const BatchArgs &A, int P, cudaStream_t st) {
-    if (A.refine_steps <= 0) return launch_cl_t<16, NT, 0>(A, P, st);
-    return launch_cl_t<16, NT, 1>(A, P, st);
+static int launch_cl_p(const BatchArgs &A, int P, cudaStream_t st) {
+    switch (P) {
+        case 2: return launch_cl_mode<NT, 2>(A, st);
+        case 4: return launch_cl_mode<NT, 4>(A, st);
+        case 8: return launch_cl_mode<NT, 8>(A, st);
+        case 16: return launch_cl_mode<NT, 16>(A, st);
+        default: return fail(TPRGB_EINVAL, "cluster of %d CTAs", P);
+    }
 }
 
 // Cluster batch: 16 equations per thread, nt in {64, 128, 256, 512} threads per
@@ -580,9 +592,9 @@ int launch_batch_cl(const BatchArgs &A, const TileConfig &cfg, cudaStream_t st) 
     int rc = cluster_parts(A.n, cfg, &P);
     if (rc) return rc;
     if (A.nsys == 0) return TPRGB_OK;
-    if (cfg.nt == 64) return launch_cl_mode<64>(A, P, st);
-    if (cfg.nt == 512) return launch_cl_mode<512>(A, P, st);
-    return cfg.nt == 128 ? launch_cl_mode<128>(A, P, st) : launch_cl_mode<256>(A, P, st);
+    if (cfg.nt == 64) return launch_cl_p<64>(A, P, st);
+    if (cfg.nt == 512) return launch_cl_p<512>(A, P, st);
+    return cfg.nt == 128 ? launch_cl_p<128>(A, P, st) : launch_cl_p<256>(A, P, st);
 }
 
 int cluster_parts(int n, const TileConfig &cfg, int *P) {

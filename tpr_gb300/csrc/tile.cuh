@@ -2,8 +2,9 @@
 // kernel: a CTA of NT threads solves either several whole systems (T = n / L
 // threads each) or one part of a system that spans several CTAs.  The parts
 // exchange their boundary rows through global scratch at counter barriers
-// (queue kernel) or through distributed shared memory with st.async onto
-// each part's row mbarriers (thread-block clusters).
+// (queue kernel), or every warp sends its segment rows through distributed
+// shared memory with st.async onto each part's row mbarriers (thread-block
+// clusters).
 #pragma once
 
 #include "cluster.cuh"
@@ -36,17 +37,22 @@ struct Smem {
     int ok;
 };
 
-// Cluster parts' boundary rows as every CTA of a cluster holds them:
-// [parity][part][row 0 / 1], (a, c, d, 0) per row.
-constexpr int kClusterRowSlots = 2 * 16 * 2;
+// Cluster parts' segment rows as every CTA of a cluster holds them:
+// [parity][segment][row F / E], (a, c, d, 0) per row, where segment g =
+// part * W + warp is the g-th 32-lane warp segment of the system (W warps
+// per part).
+template <int NT, int P>
+constexpr int cluster_row_slots() {
+    return 2 * (NT / 32) * P * 2;
+}
 
 // Multi-CTA system context.  on = 1: the parts are CTAs of a persistent
 // grid meeting at counter barriers in global scratch (per system: counter,
 // then rows [2 parity][32 parts][8 floats] and edges [2 parity][32 parts][4
 // floats]); on = 2: the parts are the CTAs of one thread-block cluster,
-// exchanging rows through distributed shared memory (crows: this CTA's
-// kClusterRowSlots-entry row buffer; rbar: its two row barriers, one per
-// parity; cstatus: timeout record (code, site, detail)).
+// exchanging segment rows through distributed shared memory (crows: this
+// CTA's row buffer of cluster_row_slots entries; rbar: its two row
+// barriers, one per parity; cstatus: timeout record (code, site, detail)).
 struct Part {
     int on, P, p;
     float4 *crows;
@@ -109,11 +115,119 @@ __device__ bool part_barrier(Part &pc, Smem<NT> &sm, int where) {
     return sm.ok != 0;
 }
 
+// Levels 2 and 3 of a system spread over the P CTAs of a thread-block
+// cluster, as one reduction.  After level 1 every warp of every part holds
+// its segment's two boundary rows (F on lane 0, E on lane 31); in the
+// order F_0, E_0, F_1, E_1, ... of all W * P segments of the system these
+// rows form a tridiagonal system with unit diagonal (2 W P rows).  Each
+// warp sends its two rows straight into every part's row buffer with
+// st.async, completing 32 bytes on that part's row mbarrier of the round's
+// parity, so no CTA barrier and no separate level-2 pass come before the
+// exchange.  Warp 0 of each part waits (bounded) for all W P segments,
+// then solves the whole reduced system redundantly: J = W P / 32 segments
+// per lane (2J rows, the thread-level partition elimination of level 0 on
+// unit-diagonal rows), a warp-wide reduction over K lanes, the top block,
+// and back.  It writes the first / last unknowns of its own W segments and
+// the neighbouring parts' edge unknowns to shared memory; the caller's CTA
+// barrier hands them to the other warps.
+//
+// Slot reuse: the rows of a parity are overwritten two rounds later.  A
+// warp sends round r + 2 only after its part's round r + 1 exchange, which
+// needs every part's round r + 1 rows, which each part's warps send only
+// after their CTA barrier of round r -- after warp 0 there has read the
+// round r rows.  The same ordering puts every round r + 2 byte after the
+// round r phase of the barrier completed.
+template <int NT, int P, int NTS>
+__device__ __forceinline__ void cluster_levels23(const Row &R0, const Row &R1,
+                                                 Smem<NTS> &sm, Part &pc) {
+    constexpr int W = NT / 32;       // warp segments per part
+    constexpr int S = W * P;         // segments of the system
+    constexpr int K = S < 32 ? S : 32;  // lanes of the reduction
+    constexpr int J = S / K;         // segments per lane
+    static_assert(S % K == 0 && J >= 1, "segments per lane");
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int warp = tid >> 5;
+    const unsigned par = pc.round & 1u;
+    // every warp: its two rows to slot (p W + warp) of every part's buffer
+    {
+        const float a0 = __shfl_sync(0xffffffffu, R0.a, 0);
+        const float c0 = __shfl_sync(0xffffffffu, R0.c, 0);
+        const float d0 = __shfl_sync(0xffffffffu, R0.d, 0);
+        const float a1 = __shfl_sync(0xffffffffu, R1.a, 31);
+        const float c1 = __shfl_sync(0xffffffffu, R1.c, 31);
+        const float d1 = __shfl_sync(0xffffffffu, R1.d, 31);
+        if (warp == 0 && lane == 0) tma::mbar_expect_tx(pc.rbar + par, 32u * S);
+        if (lane < P) {
+            const int slot = (int)par * S + pc.p * W + warp;
+            const uint32_t dst = cl::map(pc.crows + slot * 2, (unsigned)lane);
+            const uint32_t bar = cl::map(pc.rbar + par, (unsigned)lane);
+            cl::st_async4(dst, make_float4(a0, c0, d0, 0.f), bar);
+            cl::st_async4(dst + 16u, make_float4(a1, c1, d1, 0.f), bar);
+        }
+    }
+    if (warp == 0) {
+        const bool in = cl::mbar_wait(pc.rbar + par, (pc.round >> 1) & 1u, kRowWaitLimit);
+        if (!in && lane == 0) {
+            atomicCAS(&pc.cstatus[0], 0u, (unsigned)TPRGB_ETIMEOUT);
+            pc.cstatus[1] = 4;
+            pc.cstatus[2] = pc.round;
+        }
+        // lane q: segments q J .. q J + J - 1 as 2J unit-diagonal rows
+        const int q = lane & (K - 1);
+        float ra[2 * J], rb[2 * J], rc[2 * J], rd[2 * J];
+        const float4 *src = pc.crows + ((int)par * S + q * J) * 2;
+#pragma unroll
+        for (int i = 0; i < 2 * J; i++) {
+            const float4 v = src[i];
+            ra[i] = v.x;
+            rb[i] = 1.0f;
+            rc[i] = v.y;
+            rd[i] = v.z;
+        }
+        Row U0, U1;
+        Chunk<2 * J> ck;
+        if constexpr (J > 1) {
+            hier::level0<2 * J>(ra, rb, rc, rd, ck);
+            U0 = ck.F;
+            U1 = ck.E;
+        } else {
+            U0 = Row{ra[0], rc[0], rd[0]};
+            U1 = Row{ra[2 * J - 1], rc[2 * J - 1], rd[2 * J - 1]};
+        }
+        hier::seg_reduce_k<K>(U0, U1, q);
+        float zf, zl, z0, z1;
+        hier::seg_top_k<K>(U0, U1, zf, zl);
+        hier::seg_back(U0, U1, q, K, zf, zl, z0, z1);
+        float xs[2 * J];
+        if constexpr (J > 1) {
+            hier::level0_back<2 * J>(ck, z0, z1, xs);
+        } else {
+            xs[0] = z0;
+            xs[2 * J - 1] = z1;
+        }
+        // this part's segments and the neighbouring parts' edge unknowns
+        const int g0 = pc.p * W;
+        if (lane < K) {
+#pragma unroll
+            for (int j = 0; j < J; j++) {
+                const int g = q * J + j;
+                if (g >= g0 && g < g0 + W) sm.x[g - g0] = make_float2(xs[2 * j], xs[2 * j + 1]);
+                if (g == g0 - 1) sm.part_nb.x = xs[2 * j + 1];
+                if (g == g0 + W) sm.part_nb.y = xs[2 * j];
+            }
+        }
+        if (lane == 0 && pc.p == 0) sm.part_nb.x = 0.f;
+        if (lane == 0 && pc.p == P - 1) sm.part_nb.y = 0.f;
+    }
+    pc.round++;
+}
+
 // Hierarchical solve.  T: threads of this system inside the CTA (T <= NT;
 // T == NT for a part of a multi-CTA system), a compile-time power of two so
 // that segment widths and lane arithmetic fold to constants.  All threads
 // of the CTA call this (it has CTA barriers when T > 32).
-template <int L, int NT, int T>
+template <int L, int NT, int T, int PP = 0>
 __device__ __forceinline__ void solve(const float (&a)[L], const float (&b)[L],
                                       const float (&c)[L], const float (&d)[L],
                                       float (&x)[L], Smem<NT> &sm, Part &pc) {
@@ -128,6 +242,25 @@ __device__ __forceinline__ void solve(const float (&a)[L], const float (&b)[L],
     float xf, xl;
     if (T <= 32) {
         hier::seg_top_k<K>(R0, R1, xf, xl);
+    } else if constexpr (PP > 0) {
+        // a part of a system on a thread-block cluster of PP CTAs
+        // (T == NT): levels 2 and 3 as one reduction
+        cluster_levels23<NT, PP>(R0, R1, sm, pc);
+        __syncthreads();
+        const float2 v = sm.x[tid >> 5];
+        xf = v.x;
+        xl = v.y;
+        const float2 nb = sm.part_nb;
+        if (pc.nsolve == 0) {
+            pc.nb_hm = nb.x;
+            pc.nb_lm = 0.f;
+            pc.nb_hp = nb.y;
+            pc.nb_lp = 0.f;
+        } else {
+            pc.nb_lm += nb.x;
+            pc.nb_lp += nb.y;
+        }
+        pc.nsolve++;
     } else {
         constexpr int W = T > 32 ? T / 32 : 1;
         const int warp = tid >> 5;
@@ -163,72 +296,28 @@ __device__ __forceinline__ void solve(const float (&a)[L], const float (&b)[L],
                 }
                 hier::seg_reduce_k<W>(S0, S1, q2);
             }
-            // level 3: this CTA's two boundary rows -> scratch (global
-            // memory, or slot p of every cluster CTA's row buffer), barrier,
-            // every part solves the 2P-row system redundantly
+            // level 3 (persistent queue kernel): this CTA's two boundary
+            // rows -> global scratch, counter barrier, every part solves the
+            // 2P-row system redundantly
             const unsigned par = pc.round & 1u;
-            if (pc.on == 2) {
-                // lane j stores the two rows into slot p of CTA j's buffer
-                // with st.async, completing 32 bytes on CTA j's row barrier
-                // of this parity; warp 0 then waits (bounded) until all P
-                // parts' rows are in, and reads them locally.  No cluster
-                // barrier: the other warps wait for warp 0 at the CTA
-                // barrier below, and nobody waits for this CTA's earlier
-                // global stores.  Slots and barrier of a parity are reused
-                // two rounds later; a part gets there only after receiving
-                // every part's rows of the round in between, which each
-                // part sends after it has read this round's rows.
-                if (warp == 0) {
-                    const float a0 = __shfl_sync(0xffffffffu, S0.a, 0);
-                    const float c0 = __shfl_sync(0xffffffffu, S0.c, 0);
-                    const float d0 = __shfl_sync(0xffffffffu, S0.d, 0);
-                    const float a1 = __shfl_sync(0xffffffffu, S1.a, W - 1);
-                    const float c1 = __shfl_sync(0xffffffffu, S1.c, W - 1);
-                    const float d1 = __shfl_sync(0xffffffffu, S1.d, W - 1);
-                    if (lane == 0) tma::mbar_expect_tx(pc.rbar + par, 32u * (unsigned)pc.P);
-                    if (lane < pc.P) {
-                        const uint32_t dst =
-                            cl::map(pc.crows + (par * 16 + pc.p) * 2, (unsigned)lane);
-                        const uint32_t bar = cl::map(pc.rbar + par, (unsigned)lane);
-                        cl::st_async4(dst, make_float4(a0, c0, d0, 0.f), bar);
-                        cl::st_async4(dst + 16u, make_float4(a1, c1, d1, 0.f), bar);
-                    }
-                    const bool in = cl::mbar_wait(pc.rbar + par, (pc.round >> 1) & 1u,
-                                                  kRowWaitLimit);
-                    if (!in && lane == 0) {
-                        atomicCAS(&pc.cstatus[0], 0u, (unsigned)TPRGB_ETIMEOUT);
-                        pc.cstatus[1] = 4;
-                        pc.cstatus[2] = pc.round;
-                    }
-                }
-                pc.round++;
-            } else {
-                if (warp == 0 && lane == 0) {
-                    float4 *dst = reinterpret_cast<float4 *>(pc.rows + (par * 32 + pc.p) * 8);
-                    __stcg(dst, make_float4(S0.a, S0.c, S0.d, 0.f));
-                    writer_fence();
-                }
-                if (warp == 0 && lane == W - 1) {
-                    float4 *dst = reinterpret_cast<float4 *>(pc.rows + (par * 32 + pc.p) * 8 + 4);
-                    __stcg(dst, make_float4(S1.a, S1.c, S1.d, 0.f));
-                    writer_fence();
-                }
-                part_barrier<NT>(pc, sm, 1);
+            if (warp == 0 && lane == 0) {
+                float4 *dst = reinterpret_cast<float4 *>(pc.rows + (par * 32 + pc.p) * 8);
+                __stcg(dst, make_float4(S0.a, S0.c, S0.d, 0.f));
+                writer_fence();
             }
+            if (warp == 0 && lane == W - 1) {
+                float4 *dst = reinterpret_cast<float4 *>(pc.rows + (par * 32 + pc.p) * 8 + 4);
+                __stcg(dst, make_float4(S1.a, S1.c, S1.d, 0.f));
+                writer_fence();
+            }
+            part_barrier<NT>(pc, sm, 1);
             if (warp == 0) {
                 const int P = pc.P;
                 Row U0{0.f, 0.f, 0.f}, U1{0.f, 0.f, 0.f};
                 if (lane < P) {
-                    float4 v0, v1;
-                    if (pc.on == 2) {
-                        const float4 *src = pc.crows + (par * 16 + lane) * 2;
-                        v0 = src[0];
-                        v1 = src[1];
-                    } else {
-                        const float4 *src = reinterpret_cast<const float4 *>(pc.rows + (par * 32 + lane) * 8);
-                        v0 = __ldcg(src);
-                        v1 = __ldcg(src + 1);
-                    }
+                    const float4 *src =
+                        reinterpret_cast<const float4 *>(pc.rows + (par * 32 + lane) * 8);
+                    const float4 v0 = __ldcg(src), v1 = __ldcg(src + 1);
                     U0 = Row{v0.x, v0.y, v0.z};
                     U1 = Row{v1.x, v1.y, v1.z};
                 }
@@ -530,7 +619,8 @@ struct NoHook {
 // thread right after the tile's last read of the staged arrays (before the
 // last solve's reduction), so a one-stage kernel can start loading its next
 // tile there; the hook synchronises the CTA itself.
-template <int L, int NT, int T, int MODE, bool SW = false, typename Hook = NoHook>
+template <int L, int NT, int T, int MODE, bool SW = false, typename Hook = NoHook,
+          int PP = 0>
 __device__ __forceinline__ bool run_tile_smem(
     const float *sa, const float *sb, const float *sc, const float *sd,
     const unsigned (&off)[L / 4], void *__restrict__ gx, long long base,
@@ -568,7 +658,7 @@ __device__ __forceinline__ bool run_tile_smem(
         float a[L], b[L], c[L], d[L];
         load4(a, b, c, d);
         if (!refine) stage_free();
-        solve<L, NT, T>(a, b, c, d, xh, sm, pc);
+        solve<L, NT, T, PP>(a, b, c, d, xh, sm, pc);
     }
     float xlo[L];
 #pragma unroll
@@ -589,7 +679,7 @@ __device__ __forceinline__ bool run_tile_smem(
                 float a[L], b[L], c[L], d[L];
                 load4(a, b, c, d);
                 if (step == refine_steps - 1) stage_free();
-                solve<L, NT, T>(a, b, c, r, dx, sm, pc);
+                solve<L, NT, T, PP>(a, b, c, r, dx, sm, pc);
             }
 #pragma unroll
             for (int i = 0; i < L; i++) xlo[i] += dx[i];
