@@ -189,6 +189,11 @@ def test_cluster_kernel(cuda, port, n, nt, nsys):
                       threads_per_cta=nt, variant=B.CLUSTER)
     worst, _ = _err(port, bt, xp)
     assert worst <= 1e-5, worst
+    # native FP64 residual (x accumulated in FP64)
+    xd = B.solve_host(bt, refine_steps=1, residual=B.RESID_F64, eq_per_thread=16,
+                      threads_per_cta=nt, variant=B.CLUSTER)
+    worst, _ = _err(port, bt, xd)
+    assert worst <= 1e-9, worst
     import ctypes
     code = ctypes.c_uint()
     assert B.load().tprgb_batch_status(ctypes.byref(code), 1) == 0
@@ -196,10 +201,14 @@ def test_cluster_kernel(cuda, port, n, nt, nsys):
 
 
 def test_cluster_default_and_rejects(cuda, port):
-    """Above 8192 equations the default tile is the cluster variant; sizes
-    that need more than 16 or fewer than 2 CTAs are refused."""
+    """Above 8192 equations the default tile is the cluster variant (with
+    either residual); sizes that need more than 16 or fewer than 2 CTAs are
+    refused."""
     bt = G.uniform_batch(2, 32768, 5, "dominant")
     x = B.solve_host(bt, refine_steps=1)
+    worst, _ = _err(port, bt, x)
+    assert worst <= 1e-9, worst
+    x = B.solve_host(bt, refine_steps=1, residual=B.RESID_F64)
     worst, _ = _err(port, bt, x)
     assert worst <= 1e-9, worst
     with pytest.raises(T.TprError):   # 32 CTAs of 2048
@@ -208,8 +217,18 @@ def test_cluster_default_and_rejects(cuda, port):
     with pytest.raises(T.TprError):   # one CTA
         B.solve_host(G.uniform_batch(2, 1024, 5, "dominant"),
                      eq_per_thread=16, threads_per_cta=64, variant=B.CLUSTER)
-    with pytest.raises(T.TprError):   # FP64 residual
-        B.solve_host(bt, refine_steps=1, residual=B.RESID_F64)
+
+
+@pytest.mark.parametrize("steps,resid", [(1, B.RESID_DF), (2, B.RESID_DF),
+                                         (2, B.RESID_F64)])
+def test_cluster_precision_stress_shape(cuda, port, steps, resid):
+    """The precision-stress generator (weakly dominant, condition numbers up
+    to about 1e4) at N = 32768 on the cluster kernel: one or two refinement
+    steps reach 1e-9 with either residual."""
+    bt = G.uniform_batch(6, 32768, 5150, "weak")
+    x = B.solve_host(bt, refine_steps=steps, residual=resid)
+    worst, _ = _err(port, bt, x)
+    assert worst <= 1e-9, worst
 
 
 @pytest.mark.parametrize("n,nsys,L,nt,v", [

@@ -123,7 +123,7 @@ TPRGB_API int tprgb_batch_solve(int nsys, int n, const float *d_a,
     const bool sw_ok = (cfg.nt == 64 || cfg.nt == 128 || cfg.nt == 256) && n >= 32 &&
                        (cfg.L == 8 || cfg.L == 16) && !f64_resid;
     int P = 0;
-    const bool cl_ok = cfg.staged == 4 && !f64_resid && cfg.L == 16 &&
+    const bool cl_ok = cfg.staged == 4 && cfg.L == 16 &&
                        (cfg.nt == 64 || cfg.nt == 128 || cfg.nt == 256 || cfg.nt == 512) &&
                        n % (16 * cfg.nt) == 0 && (P = n / (16 * cfg.nt)) >= 2 && P <= 16;
     if (cl_ok) return launch_batch_cl(A, cfg, (cudaStream_t)stream);
@@ -137,8 +137,9 @@ TPRGB_API int tprgb_batch_solve(int nsys, int n, const float *d_a,
                     "variant %d does not serve this tile (L %d, threads %d, n %d) or residual",
                     o.variant, cfg.L, cfg.nt, n);
     // The table's kernel cannot serve this call (a caller-chosen shape, or
-    // the FP64 residual, which only the register kernel has): the register
-    // kernel, with the caller's shape where given, else one that covers n.
+    // the FP64 residual, which the staged kernels lack; the cluster and
+    // register kernels have it): the register kernel, with the caller's
+    // shape where given, else one that covers n.
     if (!o.eq_per_thread) cfg.L = n >= 16 ? 8 : 4;
     if (!o.threads_per_cta) cfg.nt = std::min(1024, std::max(128, n / cfg.L));
     cfg.staged = 0;

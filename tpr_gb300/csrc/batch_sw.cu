@@ -242,7 +242,9 @@ batch_sw(const __grid_constant__ TensorMaps tm, void *__restrict__ gx, int nsys,
 // a swizzled tensor-map load and solves its part; in each solve every warp
 // sends its segment's two boundary rows into every part's shared memory
 // (st.async onto a row mbarrier per parity) and warp 0 of each part solves
-// the system's reduced rows (tile::cluster_levels23).  Clusters
+// the system's reduced rows (tile::cluster_levels23); above 64 warp
+// segments per system each part first reduces its own rows to two and
+// only those are exchanged (tile::cluster_levels2_3).  Clusters
 // walk the batch with a stride of the number of clusters; every CTA of a
 // cluster runs the same number of systems and solves, so their row
 // exchanges pair up.  A load that times out is recorded in the status
@@ -569,6 +571,7 @@ static int launch_cl_t(const BatchArgs &A, cudaStream_t st) {
 template <int NT, int P>
 static int launch_cl_mode(const BatchArgs &A, cudaStream_t st) {
     if (A.refine_steps <= 0) return launch_cl_t<16, NT, 0, P>(A, st);
+    if (A.residual == TPRGB_RESID_F64) return launch_cl_t<16, NT, 2, P>(A, st);
     return launch_cl_t<16, NT, 1, P>(A, st);
 }
 
@@ -584,10 +587,9 @@ static int launch_cl_p(const BatchArgs &A, int P, cudaStream_t st) {
 }
 
 // Cluster batch: 16 equations per thread, nt in {64, 128, 256, 512} threads per
-// CTA, P = n / (16 nt) CTAs per system with P in {2, 4, 8, 16}.
+// CTA, P = n / (16 nt) CTAs per system with P in {2, 4, 8, 16}; plain FP32,
+// compensated FP32 residual or native FP64 residual.
 int launch_batch_cl(const BatchArgs &A, const TileConfig &cfg, cudaStream_t st) {
-    if (A.residual == TPRGB_RESID_F64 && A.refine_steps > 0)
-        return fail(TPRGB_EUNSUPPORTED, "cluster kernel has no FP64 residual mode");
     int P = 0;
     int rc = cluster_parts(A.n, cfg, &P);
     if (rc) return rc;

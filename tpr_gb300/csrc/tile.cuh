@@ -37,13 +37,14 @@ struct Smem {
     int ok;
 };
 
-// Cluster parts' segment rows as every CTA of a cluster holds them:
+// Cluster parts' rows as every CTA of a cluster holds them:
 // [parity][segment][row F / E], (a, c, d, 0) per row, where segment g =
 // part * W + warp is the g-th 32-lane warp segment of the system (W warps
-// per part).
+// per part) -- or, for systems of more than 64 segments (two-stage
+// exchange), [parity][part][row F / E] of the parts' level-2 rows.
 template <int NT, int P>
 constexpr int cluster_row_slots() {
-    return 2 * (NT / 32) * P * 2;
+    return (NT / 32) * P <= 64 ? 2 * (NT / 32) * P * 2 : 2 * P * 2;
 }
 
 // Multi-CTA system context.  on = 1: the parts are CTAs of a persistent
@@ -223,6 +224,88 @@ __device__ __forceinline__ void cluster_levels23(const Row &R0, const Row &R1,
     pc.round++;
 }
 
+// Levels 2 and 3 of a cluster part in two stages, for systems of more than
+// 64 warp segments (where the one-pass reduction's per-lane rows and 128
+// senders per round cost more than a local level 2): the W segment rows
+// of the part meet in shared memory (CTA barrier), warp 0 reduces them to
+// the part's two boundary rows (level 2), sends them into every part's row
+// buffer with st.async (completing 32 bytes on that part's row mbarrier of
+// the round's parity), waits (bounded) for all P parts' rows, solves the
+// 2P-row system (level 3), and back-substitutes level 2 into shared memory
+// for the caller's CTA barrier.  Slot reuse as for cluster_levels23: a part
+// sends round r + 2 only after receiving every part's round r + 1 rows,
+// each sent after that part read its round r rows.
+template <int NT, int P, int NTS>
+__device__ __forceinline__ void cluster_levels2_3(const Row &R0, const Row &R1,
+                                                  Smem<NTS> &sm, Part &pc) {
+    constexpr int W = NT / 32;
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int warp = tid >> 5;
+    if (lane == 0) sm.rows[warp].R0 = R0;
+    if (lane == 31) sm.rows[warp].R1 = R1;
+    __syncthreads();
+    if (warp == 0) {
+        Row S0{0.f, 0.f, 0.f}, S1{0.f, 0.f, 0.f};
+        const int q2 = lane & (W - 1);
+        if (lane < W) {
+            S0 = sm.rows[lane].R0;
+            S1 = sm.rows[lane].R1;
+        }
+        hier::seg_reduce_k<W>(S0, S1, q2);
+        const unsigned par = pc.round & 1u;
+        const float a0 = __shfl_sync(0xffffffffu, S0.a, 0);
+        const float c0 = __shfl_sync(0xffffffffu, S0.c, 0);
+        const float d0 = __shfl_sync(0xffffffffu, S0.d, 0);
+        const float a1 = __shfl_sync(0xffffffffu, S1.a, W - 1);
+        const float c1 = __shfl_sync(0xffffffffu, S1.c, W - 1);
+        const float d1 = __shfl_sync(0xffffffffu, S1.d, W - 1);
+        if (lane == 0) tma::mbar_expect_tx(pc.rbar + par, 32u * P);
+        if (lane < P) {
+            const uint32_t dst = cl::map(pc.crows + ((int)par * P + pc.p) * 2, (unsigned)lane);
+            const uint32_t bar = cl::map(pc.rbar + par, (unsigned)lane);
+            cl::st_async4(dst, make_float4(a0, c0, d0, 0.f), bar);
+            cl::st_async4(dst + 16u, make_float4(a1, c1, d1, 0.f), bar);
+        }
+        const bool in = cl::mbar_wait(pc.rbar + par, (pc.round >> 1) & 1u, kRowWaitLimit);
+        if (!in && lane == 0) {
+            atomicCAS(&pc.cstatus[0], 0u, (unsigned)TPRGB_ETIMEOUT);
+            pc.cstatus[1] = 4;
+            pc.cstatus[2] = pc.round;
+        }
+        Row U0{0.f, 0.f, 0.f}, U1{0.f, 0.f, 0.f};
+        if (lane < P) {
+            const float4 *src = pc.crows + ((int)par * P + lane) * 2;
+            const float4 v0 = src[0], v1 = src[1];
+            U0 = Row{v0.x, v0.y, v0.z};
+            U1 = Row{v1.x, v1.y, v1.z};
+        }
+        const int q3 = lane & (P - 1);
+        hier::seg_reduce_k<P>(U0, U1, q3);
+        float zf, zl, z0, z1;
+        hier::seg_top_k<P>(U0, U1, zf, zl);
+        hier::seg_back(U0, U1, q3, P, zf, zl, z0, z1);
+        const float yf = __shfl_sync(0xffffffffu, z0, pc.p);
+        const float yl = __shfl_sync(0xffffffffu, z1, pc.p);
+        // the neighbouring parts' edge unknowns for the next residual
+        const float pl = __shfl_sync(0xffffffffu, z1, pc.p > 0 ? pc.p - 1 : 0);
+        const float nf = __shfl_sync(0xffffffffu, z0, pc.p < P - 1 ? pc.p + 1 : 0);
+        if (lane == 0)
+            sm.part_nb = make_float2(pc.p > 0 ? pl : 0.f, pc.p < P - 1 ? nf : 0.f);
+        float y0, y1;
+        hier::seg_back(S0, S1, q2, W, yf, yl, y0, y1);
+        if (lane < W) sm.x[lane] = make_float2(y0, y1);
+    }
+    pc.round++;
+}
+
+// Which cluster exchange a (threads per CTA, parts) shape uses: the
+// one-pass reduction up to 64 warp segments per system, two stages above.
+template <int NT, int P>
+constexpr bool cluster_one_pass() {
+    return (NT / 32) * P <= 64;
+}
+
 // Hierarchical solve.  T: threads of this system inside the CTA (T <= NT;
 // T == NT for a part of a multi-CTA system), a compile-time power of two so
 // that segment widths and lane arithmetic fold to constants.  All threads
@@ -245,7 +328,10 @@ __device__ __forceinline__ void solve(const float (&a)[L], const float (&b)[L],
     } else if constexpr (PP > 0) {
         // a part of a system on a thread-block cluster of PP CTAs
         // (T == NT): levels 2 and 3 as one reduction
-        cluster_levels23<NT, PP>(R0, R1, sm, pc);
+        if constexpr (cluster_one_pass<NT, PP>())
+            cluster_levels23<NT, PP>(R0, R1, sm, pc);
+        else
+            cluster_levels2_3<NT, PP>(R0, R1, sm, pc);
         __syncthreads();
         const float2 v = sm.x[tid >> 5];
         xf = v.x;
@@ -606,6 +692,16 @@ __device__ __forceinline__ void swizzled_offsets(int tid, unsigned (&off)[L / 4]
     for (int j = 0; j < L / 4; j++) off[j] = b0 ^ ((((unsigned)j) ^ r7) << 4);
 }
 
+// Unit u (equations 4u .. 4u + 3) of this thread's chunk of one staged
+// array: at byte offset off[u] from the region's base (swizzled), or the
+// u-th float4 of the thread's contiguous chunk.
+template <int L, bool SW>
+__device__ __forceinline__ float4 unit_at(const float *base, const unsigned (&off)[L / 4],
+                                          int u) {
+    if (SW) return *reinterpret_cast<const float4 *>(reinterpret_cast<const char *>(base) + off[u]);
+    return reinterpret_cast<const float4 *>(base)[u];
+}
+
 // No-op stage-free hook (run_tile_smem's default).
 struct NoHook {
     __device__ __forceinline__ void operator()() const {}
@@ -613,7 +709,9 @@ struct NoHook {
 
 // Same computation as run_tile, but a, b, c, d are re-read from shared
 // memory each time they are needed instead of being held in registers
-// through the refinement.  SW = false: sa..sd point at this thread's
+// through the refinement.  MODE: 0 plain FP32, 1 refinement with the
+// compensated FP32 residual, 2 refinement with the native FP64 residual
+// (x accumulated in FP64).  SW = false: sa..sd point at this thread's
 // contiguous chunk; SW = true: sa..sd are the array regions' bases and off
 // holds the chunk's swizzled unit offsets.  stage_free() is called by every
 // thread right after the tile's last read of the staged arrays (before the
@@ -652,13 +750,82 @@ __device__ __forceinline__ bool run_tile_smem(
         if (first_eq) a[0] = 0.f;
         if (last_eq) c[L - 1] = 0.f;
     };
-    const bool refine = MODE == 1 && refine_steps > 0;
+    const bool refine = MODE != 0 && refine_steps > 0;
     float xh[L];
     {
         float a[L], b[L], c[L], d[L];
         load4(a, b, c, d);
         if (!refine) stage_free();
         solve<L, NT, T, PP>(a, b, c, d, xh, sm, pc);
+    }
+    if constexpr (MODE == 2) {
+        // native FP64 residual: x accumulated in FP64, the residual
+        // r = d - A x formed by three DFMAs on the exactly converted
+        // coefficients and rounded once to FP32 for the correction solve
+        double xd[L];
+#pragma unroll
+        for (int i = 0; i < L; i++) xd[i] = (double)xh[i];
+        for (int step = 0; step < refine_steps; step++) {
+            // the chunk's edge values as (hi, lo) FP32 pairs for the
+            // neighbour exchange
+            const float fh = (float)xd[0], fl = (float)(xd[0] - (double)fh);
+            const float lh = (float)xd[L - 1], ll = (float)(xd[L - 1] - (double)lh);
+            float hm, lm, hp, lp;
+            neighbours<NT, T>(fh, lh, fl, ll, t, hm, lm, hp, lp, sm, pc);
+            const double xm = (double)hm + (double)lm;
+            const double xp = (double)hp + (double)lp;
+            float r[L];
+            // four equations at a time (one 16-byte unit of each array), so
+            // that only one unit of the coefficients is live beside x
+#pragma unroll
+            for (int u = 0; u < L / 4; u++) {
+                float4 ua = make_float4(0.f, 0.f, 0.f, 0.f), ub = make_float4(1.f, 1.f, 1.f, 1.f);
+                float4 uc = ua, ud = ua;
+                if (active) {
+                    ua = unit_at<L, SW>(sa, off, u);
+                    ub = unit_at<L, SW>(sb, off, u);
+                    uc = unit_at<L, SW>(sc, off, u);
+                    ud = unit_at<L, SW>(sd, off, u);
+                }
+                const float ea[4] = {ua.x, ua.y, ua.z, ua.w}, eb[4] = {ub.x, ub.y, ub.z, ub.w};
+                const float ec[4] = {uc.x, uc.y, uc.z, uc.w}, ed[4] = {ud.x, ud.y, ud.z, ud.w};
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int i = 4 * u + j;
+                    const float ai = (i == 0 && first_eq) ? 0.f : ea[j];
+                    const float ci = (i == L - 1 && last_eq) ? 0.f : ec[j];
+                    double rr = fma(-(double)eb[j], xd[i], (double)ed[j]);
+                    rr = fma(-(double)ai, i > 0 ? xd[i - 1] : xm, rr);
+                    rr = fma(-(double)ci, i < L - 1 ? xd[i + 1] : xp, rr);
+                    r[i] = (float)rr;
+                }
+            }
+            float dx[L];
+            {
+                float a[L], b[L], c[L], d[L];
+                load4(a, b, c, d);
+                if (step == refine_steps - 1) stage_free();
+                solve<L, NT, T, PP>(a, b, c, r, dx, sm, pc);
+            }
+#pragma unroll
+            for (int i = 0; i < L; i++) xd[i] += (double)dx[i];
+        }
+        if (!active) return true;
+        bool finite = true;
+#pragma unroll
+        for (int i = 0; i < L; i++) finite = finite && isfinite(xd[i]);
+        if (x_f64) {
+            double2 *o = reinterpret_cast<double2 *>((double *)gx + base);
+#pragma unroll
+            for (int i = 0; i < L / 2; i++) o[i] = make_double2(xd[2 * i], xd[2 * i + 1]);
+        } else {
+            float4 *o = reinterpret_cast<float4 *>((float *)gx + base);
+#pragma unroll
+            for (int i = 0; i < L / 4; i++)
+                o[i] = make_float4((float)xd[4 * i], (float)xd[4 * i + 1],
+                                   (float)xd[4 * i + 2], (float)xd[4 * i + 3]);
+        }
+        return finite;
     }
     float xlo[L];
 #pragma unroll
