@@ -410,6 +410,17 @@ TPRGB_API int tprgb_cusparse_gtsv(int prec, int n, const void *a,
                                   const void *diag, const void *c,
                                   const void *rhs, void *x, float *device_ms);
 
+/* Times `iters` host round trips of one system through a solver handle --
+ * set_tridiagonal_system (3-argument with diag NULL, else 4-argument),
+ * solve, get_ans -- in C++, after one untimed warm-up; *us_per_solve = the
+ * mean microseconds per round trip.  The reference's timed loop
+ * (src/pm.cpp:160-194) times its CPU solvers the same way (solve +
+ * get_ans per iteration); this includes the setter's copy as well.  No
+ * reference counterpart (a measurement helper). */
+TPRGB_API int tprgb_time_roundtrip(tprgb_solver *h, const void *a, const void *diag,
+                                   const void *c, const void *rhs, void *x, int iters,
+                                   double *us_per_solve);
+
 /* ---- diagnostics ------------------------------------------------------- */
 /* Status word of the TMA-staged batched kernel: *code = TPRGB_ETIMEOUT if a
  * bounded wait gave up since the last reset (reset != 0 clears it). */

@@ -58,6 +58,8 @@ def _declare(L):
         "tprgb_solve": (i, [vp, C.POINTER(i)]),
         "tprgb_get_ans": (i, [vp, vp]),
         "tprgb_release_cached": (i, []),
+        "tprgb_time_roundtrip": (i, [vp, vp, vp, vp, vp, vp, i,
+                                     C.POINTER(C.c_double)]),
         "tprgb_cusparse_gtsv": (i, [i, i, vp, vp, vp, vp, vp,
                                     C.POINTER(C.c_float)]),
     }

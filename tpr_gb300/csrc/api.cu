@@ -4,6 +4,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <chrono>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -37,6 +38,9 @@ int launch_ref(int kind, int nsys, int n, int s, int prec, const void *a,
                void *work, cudaStream_t st);
 int launch_normalize(int prec, long long neq, void *a, const void *diag,
                      void *c, void *r, cudaStream_t st);
+bool ref_direct_ok(int kind, int n, int s, int prec);
+int launch_ref_direct(int kind, int n, int s, int prec, const void *a, const void *diag,
+                      const void *c, const void *r, void *x, cudaStream_t st);
 
 static int flops_of(int kind, int n, int s) {
     int ln = ilog2(n);
@@ -65,13 +69,22 @@ struct tprgb_solver {
     int kind, n, s, prec;
     size_t esz;
     void *d_a = nullptr, *d_c = nullptr, *d_r = nullptr, *d_diag = nullptr;
-    // pinned staging (a, c, rhs, diag | x) so one solve costs one host
-    // synchronisation (in get_ans)
+    // pinned, device-mapped staging (a, c, rhs, diag | x) so one solve costs
+    // one host synchronisation (in get_ans)
     unsigned char *h_stage = nullptr, *h_x = nullptr;
-    cudaEvent_t staged = nullptr;  // the last upload has left h_stage
+    unsigned char *hd_stage = nullptr;  // the staging's device address
+    cudaEvent_t staged = nullptr;  // the last solve has left h_stage
     void *d_x = nullptr, *d_work = nullptr;
     cudaStream_t stream = nullptr;
     bool has_system = false;
+    // One-launch path (TPR / PTPR on a thread-block cluster, 2..16 slices
+    // of the fused shape): the kernel reads the system, divides by the
+    // diagonal and writes x in the pinned staging itself -- no copies, one
+    // launch per solve (the GPU reaches host memory over the chip-to-chip
+    // link; for one small system that beats two copies and a separate
+    // normalising launch).  Other shapes upload, normalise and download.
+    bool direct = false;
+    bool use_diag = false;
 };
 
 extern "C" {
@@ -173,7 +186,9 @@ TPRGB_API int tprgb_create(int kind, int n, int s, int prec,
         free_handle(h);
         return cuda_fail(e, "cudaMalloc(solver buffers)");
     }
-    e = cudaHostAlloc((void **)&h->h_stage, 5 * (size_t)n * h->esz, 0);
+    e = cudaHostAlloc((void **)&h->h_stage, 5 * (size_t)n * h->esz, cudaHostAllocMapped);
+    if (e == cudaSuccess)
+        e = cudaHostGetDevicePointer((void **)&h->hd_stage, h->h_stage, 0);
     if (e == cudaSuccess)
         e = cudaEventCreateWithFlags(&h->staged, cudaEventDisableTiming);
     if (e != cudaSuccess) {
@@ -181,6 +196,7 @@ TPRGB_API int tprgb_create(int kind, int n, int s, int prec,
         return cuda_fail(e, "pinned staging");
     }
     h->h_x = h->h_stage + 4 * (size_t)n * h->esz;
+    h->direct = ref_direct_ok(kind, n, s, prec);
     char *p = (char *)h->d_a;
     h->d_c = p + 1 * (size_t)n * h->esz;
     h->d_r = p + 2 * (size_t)n * h->esz;
@@ -218,6 +234,11 @@ TPRGB_API int tprgb_set_system(tprgb_solver *h, const void *a,
     memcpy(h->h_stage + bytes, c, bytes);
     memcpy(h->h_stage + 2 * bytes, rhs, bytes);
     if (use_diag) memcpy(h->h_stage + 3 * bytes, diag, bytes);
+    h->use_diag = use_diag;
+    if (h->direct) {  // the solve reads the staging itself
+        h->has_system = true;
+        return TPRGB_OK;
+    }
     // device layout a, c, rhs, diag is contiguous: one copy
     TPRGB_CUDA(cudaMemcpyAsync(h->d_a, h->h_stage, (use_diag ? 4 : 3) * bytes,
                                cudaMemcpyHostToDevice, h->stream));
@@ -236,9 +257,21 @@ TPRGB_API int tprgb_solve(tprgb_solver *h, int *flops) {
     if (!h->has_system)
         return fail(TPRGB_EINVAL, "set_tridiagonal_system was not called");
     // enqueued only: get_ans waits for it (and reports a failed launch)
-    int rc = launch_ref(h->kind, 1, h->n, h->s, h->prec, h->d_a, h->d_c,
+    int rc;
+    if (h->direct) {
+        const size_t bytes = (size_t)h->n * h->esz;
+        rc = launch_ref_direct(h->kind, h->n, h->s, h->prec, h->hd_stage,
+                               h->use_diag ? h->hd_stage + 3 * bytes : nullptr,
+                               h->hd_stage + bytes, h->hd_stage + 2 * bytes,
+                               h->hd_stage + 4 * bytes, h->stream);
+        if (rc) return rc;
+        // the next set_system waits until this solve has read the staging
+        TPRGB_CUDA(cudaEventRecord(h->staged, h->stream));
+    } else {
+        rc = launch_ref(h->kind, 1, h->n, h->s, h->prec, h->d_a, h->d_c,
                         h->d_r, h->d_x, h->n, h->d_work, h->stream);
-    if (rc) return rc;
+        if (rc) return rc;
+    }
     if (flops) *flops = flops_of(h->kind, h->n, h->s);
     return TPRGB_OK;
 }
@@ -247,10 +280,33 @@ TPRGB_API int tprgb_get_ans(tprgb_solver *h, void *x) {
     if (!h) return fail(TPRGB_EINVAL, "handle is NULL");
     if (!x) return fail(TPRGB_EINVAL, "x is NULL");
     const size_t bytes = (size_t)h->n * h->esz;
-    TPRGB_CUDA(cudaMemcpyAsync(h->h_x, h->d_x, bytes, cudaMemcpyDeviceToHost,
-                               h->stream));
+    if (!h->direct)
+        TPRGB_CUDA(cudaMemcpyAsync(h->h_x, h->d_x, bytes, cudaMemcpyDeviceToHost,
+                                   h->stream));
     TPRGB_CUDA(cudaStreamSynchronize(h->stream));
     memcpy(x, h->h_x, bytes);
+    return TPRGB_OK;
+}
+
+TPRGB_API int tprgb_time_roundtrip(tprgb_solver *h, const void *a, const void *diag,
+                                   const void *c, const void *rhs, void *x, int iters,
+                                   double *us_per_solve) {
+    if (!h) return fail(TPRGB_EINVAL, "handle is NULL");
+    if (!us_per_solve || iters <= 0)
+        return fail(TPRGB_EINVAL, "iters must be positive and us_per_solve set");
+    auto once = [&]() {
+        int rc = tprgb_set_system(h, a, diag, c, rhs);
+        if (!rc) rc = tprgb_solve(h, nullptr);
+        if (!rc) rc = tprgb_get_ans(h, x);
+        return rc;
+    };
+    int rc = once();  // warm-up
+    if (rc) return rc;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int i = 0; i < iters && !rc; i++) rc = once();
+    const auto t1 = std::chrono::steady_clock::now();
+    if (rc) return rc;
+    *us_per_solve = std::chrono::duration<double, std::micro>(t1 - t0).count() / iters;
     return TPRGB_OK;
 }
 

@@ -16,8 +16,11 @@
 //  * sliced (systems too large for one CTA's shared memory): stage 1 per
 //    slice CTA -> global workspace, stage 2 in one CTA per system, stage 3
 //    per slice CTA.  Three launches on one stream, no grid sync.
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <mutex>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -92,17 +95,90 @@ __device__ void ptpr_stage1(T *a, T *c, T *r, int n, int s) {
     }
 }
 
+// PTPR stage 1 on one slice of s rows, EPT rows per thread (s <= EPT *
+// blockDim.x), double-buffered: step p reads one copy of a, c, r and writes
+// the other, so a step needs one CTA barrier.  The per-row arithmetic is
+// ptpr_stage1's.  Returns 1 when the result is in the second copy (an odd
+// number of steps), else 0.
+template <typename T, int EPT>
+__device__ int ptpr_stage1_slice(T *a0, T *c0, T *r0, T *a1, T *c1, T *r1, int s) {
+    const int ls = ilog2(s);
+    for (int p = 1; p <= ls; p++) {
+        const int u = 1 << (p - 1);
+        const bool odd = (p & 1) == 0;  // step p reads copy (p - 1) & 1
+        const T *a = odd ? a1 : a0, *c = odd ? c1 : c0, *r = odd ? r1 : r0;
+        T *oa = odd ? a0 : a1, *oc = odd ? c0 : c1, *orr = odd ? r0 : r1;
+#pragma unroll
+        for (int e = 0; e < EPT; e++) {
+            const int i = threadIdx.x + e * blockDim.x;
+            if (i < s) {
+                T na, nc, nr;
+                if (i < u)
+                    upd_upper(a, c, r, i, i + u, na, nc, nr);
+                else if (i <= s - 1 - u)
+                    upd_mid(a, c, r, i - u, i, i + u, na, nc, nr);
+                else
+                    upd_lower(a, c, r, i - u, i, na, nc, nr);
+                oa[i] = na;
+                oc[i] = nc;
+                orr[i] = nr;
+            }
+        }
+        __syncthreads();
+    }
+    return ls & 1;
+}
+
+// TPR stage 1 on one slice of s rows, EPT rows per thread.  At level p >= 2
+// the rows updated (li % 2^p in {0, 2^p - 1}) are never the neighbours
+// (li +- 2^(p-1)) of an updated row, so a level writes in place after its
+// reads with one CTA barrier; level 1 updates every row and keeps two.  The
+// per-row arithmetic is tpr_stage1's.
+template <typename T, int EPT>
+__device__ void tpr_stage1_slice(T *a, T *c, T *r, int s) {
+    const int ls = ilog2(s);
+    for (int p = 1; p <= ls; p++) {
+        const int u = 1 << (p - 1), p2k = 1 << p;
+        T na[EPT], nc[EPT], nr[EPT];
+        bool sel[EPT];
+#pragma unroll
+        for (int e = 0; e < EPT; e++) {
+            const int i = threadIdx.x + e * blockDim.x;
+            sel[e] = i < s && (((i & (p2k - 1)) == 0) || (((i + 1) & (p2k - 1)) == 0));
+            if (sel[e]) {
+                if (i == 0)
+                    upd_upper(a, c, r, i, i + u, na[e], nc[e], nr[e]);
+                else if (i == s - 1)
+                    upd_lower(a, c, r, i - u, i, na[e], nc[e], nr[e]);
+                else
+                    upd_mid(a, c, r, i - u, i, i + u, na[e], nc[e], nr[e]);
+            }
+        }
+        if (p == 1) __syncthreads();
+#pragma unroll
+        for (int e = 0; e < EPT; e++) {
+            const int i = threadIdx.x + e * blockDim.x;
+            if (sel[e]) {
+                a[i] = na[e];
+                c[i] = nc[e];
+                r[i] = nr[e];
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // TPR stage 1 tree levels (src/tpr.cpp:123-230): at level p only rows with
 // li % 2^p == 0 or (li+1) % 2^p == 0 are updated.
-template <typename T>
+template <typename T, int EPT = kEpt>
 __device__ void tpr_stage1(T *a, T *c, T *r, int n, int s) {
     const int ls = ilog2(s);
     for (int p = 1; p <= ls; p++) {
         const int u = 1 << (p - 1), p2k = 1 << p;
-        T na[kEpt], nc[kEpt], nr[kEpt];
-        bool sel[kEpt];
+        T na[EPT], nc[EPT], nr[EPT];
+        bool sel[EPT];
 #pragma unroll
-        for (int e = 0; e < kEpt; e++) {
+        for (int e = 0; e < EPT; e++) {
             int i = threadIdx.x + e * blockDim.x;
             sel[e] = false;
             if (i < n) {
@@ -120,7 +196,7 @@ __device__ void tpr_stage1(T *a, T *c, T *r, int n, int s) {
         }
         __syncthreads();
 #pragma unroll
-        for (int e = 0; e < kEpt; e++) {
+        for (int e = 0; e < EPT; e++) {
             int i = threadIdx.x + e * blockDim.x;
             if (sel[e]) {
                 a[i] = na[e];
@@ -157,14 +233,14 @@ __device__ __forceinline__ void inter_eq(T ak, T ck, T rk, T akr, T ckr,
 }
 
 // PCR on m rows in shared memory (src/pcr.cpp:15-89); rhs holds x on exit.
-template <typename T>
+template <typename T, int EPT = kEpt>
 __device__ void cta_pcr(T *a, T *c, T *r, int m) {
     const int pn = ilog2(m);
     for (int p = 0; p < pn; p++) {
         const int s = 1 << p;
-        T na[kEpt], nc[kEpt], nr[kEpt];
+        T na[EPT], nc[EPT], nr[EPT];
 #pragma unroll
-        for (int e = 0; e < kEpt; e++) {
+        for (int e = 0; e < EPT; e++) {
             int k = threadIdx.x + e * blockDim.x;
             if (k < m) {
                 if (k < s) {
@@ -192,7 +268,7 @@ __device__ void cta_pcr(T *a, T *c, T *r, int m) {
         }
         __syncthreads();
 #pragma unroll
-        for (int e = 0; e < kEpt; e++) {
+        for (int e = 0; e < EPT; e++) {
             int k = threadIdx.x + e * blockDim.x;
             if (k < m) {
                 a[k] = na[e];
@@ -205,7 +281,7 @@ __device__ void cta_pcr(T *a, T *c, T *r, int m) {
 }
 
 // CR on m rows in shared memory (src/cr.cpp:23-116); solution into x.
-template <typename T>
+template <typename T, int EPT = kEpt>
 __device__ void cta_cr(T *a, T *c, T *r, T *x, int m) {
     if (m <= 1) {
         if (threadIdx.x == 0) x[0] = r[0];
@@ -216,9 +292,9 @@ __device__ void cta_cr(T *a, T *c, T *r, T *x, int m) {
     for (int p = 0; p < ln - 1; p++) {
         const int u = 1 << p, ux = 1 << (p + 1);
         const int rows = m / ux;  // rows ux-1 + ux*j, j < rows; last is m-1
-        T na[kEpt], nc[kEpt], nr[kEpt];
+        T na[EPT], nc[EPT], nr[EPT];
 #pragma unroll
-        for (int e = 0; e < kEpt; e++) {
+        for (int e = 0; e < EPT; e++) {
             int j = threadIdx.x + e * blockDim.x;
             if (j < rows) {
                 int i = ux - 1 + ux * j;
@@ -230,7 +306,7 @@ __device__ void cta_cr(T *a, T *c, T *r, T *x, int m) {
         }
         __syncthreads();
 #pragma unroll
-        for (int e = 0; e < kEpt; e++) {
+        for (int e = 0; e < EPT; e++) {
             int j = threadIdx.x + e * blockDim.x;
             if (j < rows) {
                 int i = ux - 1 + ux * j;
@@ -398,6 +474,144 @@ fused_crpcr(const T *__restrict__ ga, const T *__restrict__ gc,
         cta_cr(a, c, r, x, n);
         for (int i = threadIdx.x; i < n; i += blockDim.x) gx[base + i] = x[i];
     }
+}
+
+// One system on a thread-block cluster of m = n / s CTAs (2 <= m <= 16), CTA
+// j holding slice j: stage 1 of the m slices runs on m SMs at once.  After
+// the E_st update each CTA writes its slice's first row (E_st, updated) and
+// last row (E_ed) into every CTA's shared memory (distributed shared
+// memory, one cluster barrier); every CTA then forms the m reduced
+// equations and solves stage 2 itself -- the same arithmetic on the same
+// values, so the same bits in every CTA -- and runs stage 3 on its slice.
+// Per row the operations and their order are those of fused_tpr.  gd (may
+// be null): the diagonal, dividing a, c, r on load exactly as the 4-argument
+// setter does (normalize_kernel) -- so inputs and output may also sit in
+// pinned host memory and one launch serves a whole host round trip.
+template <typename T, int KIND, int EPT>
+__global__ void __launch_bounds__(kThreads)
+cluster_tpr(const T *__restrict__ ga, const T *__restrict__ gd,
+            const T *__restrict__ gc, const T *__restrict__ gr,
+            T *__restrict__ gx, int n, int s, long long stride) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sm = reinterpret_cast<T *>(smem_raw);
+    const int m = n / s;
+    const int j = (int)cluster.block_rank();
+    T *a = sm, *c = sm + s, *r = sm + 2 * s, *x = sm + 3 * s;
+    T *a2 = sm + 4 * s, *c2 = sm + 5 * s, *r2 = sm + 6 * s;  // PTPR's second copy
+    T *ends = sm + 7 * s;  // [m][6]: E_st (a, c, r) after the update, E_ed (a, c, r)
+    T *sa = ends + 6 * m, *sc = sa + m, *sr = sc + m, *sx = sr + m;
+    T *bk = sx + m;        // this slice's E_st before the update (PTPR)
+    const long long base = (long long)(blockIdx.x / m) * stride + (long long)j * s;
+    ga += base;
+    gc += base;
+    gr += base;
+    gx += base;
+    if (gd) gd += base;
+    auto load = [&](int i) {  // row i of the inputs, diag-normalised
+        if (gd) {
+            const T dd = gd[i];
+            a[i] = ga[i] / dd;
+            c[i] = gc[i] / dd;
+            r[i] = gr[i] / dd;
+        } else {
+            a[i] = ga[i];
+            c[i] = gc[i];
+            r[i] = gr[i];
+        }
+    };
+    for (int i = threadIdx.x; i < s; i += blockDim.x) load(i);
+    // every CTA of the cluster must have started (its shared memory
+    // exists) before any CTA writes into it: arrive now, wait just before
+    // the writes, so the barrier's latency overlaps stage 1
+    asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+    __syncthreads();
+    if (KIND == TPRGB_PTPR) {
+        if (ptpr_stage1_slice<T, EPT>(a, c, r, a2, c2, r2, s)) {
+            T *t;
+            t = a; a = a2; a2 = t;
+            t = c; c = c2; c2 = t;
+            t = r; r = r2; r2 = t;
+        }
+    } else {
+        tpr_stage1_slice<T, EPT>(a, c, r, s);
+    }
+    if (threadIdx.x == 0) {
+        if (KIND == TPRGB_PTPR) {
+            bk[0] = a[0];
+            bk[1] = c[0];
+            bk[2] = r[0];
+        }
+        est_update(a, c, r, 0, s - 1);
+    }
+    __syncthreads();
+    asm volatile("barrier.cluster.wait.aligned;" ::: "memory");
+    if (threadIdx.x < m) {  // thread q writes this slice's rows into CTA q
+        T *dst = cluster.map_shared_rank(ends, (unsigned)threadIdx.x) + 6 * j;
+        dst[0] = a[0];
+        dst[1] = c[0];
+        dst[2] = r[0];
+        dst[3] = a[s - 1];
+        dst[4] = c[s - 1];
+        dst[5] = r[s - 1];
+    }
+    cluster.sync();  // every slice's rows are in every CTA; no remote access after
+    for (int q = threadIdx.x; q < m; q += blockDim.x) {
+        const T *e = ends + 6 * q;
+        if (q < m - 1)  // E_ed of slice q with E_st of slice q + 1
+            inter_eq(e[3], e[4], e[5], e[6], e[7], e[8], sa[q], sc[q], sr[q]);
+        else {
+            sa[q] = e[3];
+            sc[q] = e[4];
+            sr[q] = e[5];
+        }
+    }
+    __syncthreads();
+    // x of the previous slice's last row (0 before the first) and of this
+    // slice's last row, from stage 2
+    T xprev, xed;
+    if (KIND == TPRGB_PTPR) {
+        cta_pcr<T, 1>(sa, sc, sr, m);  // src/ptpr.cpp:246-258 (m <= 16 rows)
+        xprev = j > 0 ? sr[j - 1] : T(0);
+        xed = sr[j];
+        if (threadIdx.x == 0) {  // restore E_st, src/ptpr.cpp:266-271
+            a[0] = bk[0];
+            c[0] = bk[1];
+            r[0] = bk[2];
+        }
+        __syncthreads();
+        // stage 3, src/ptpr.cpp:263-287
+        for (int i = threadIdx.x; i < s - 1; i += blockDim.x) {
+            T key = T(1) / c[s - 1] * (r[s - 1] - a[s - 1] * xprev - xed);
+            if (c[s - 1] == T(0)) key = T(0);
+            x[i] = r[i] - a[i] * xprev - c[i] * key;
+        }
+        if (threadIdx.x == 0) x[s - 1] = xed;
+        __syncthreads();
+    } else {
+        cta_cr<T, 1>(sa, sc, sr, sx, m);  // src/tpr.cpp:263-275 (m <= 16 rows)
+        xprev = j > 0 ? sx[j - 1] : T(0);
+        xed = sx[j];
+        // restore: even slice-local rows from the untouched inputs, odd
+        // rows keep their post-stage-1 values (src/tpr.cpp:236-325,381-387)
+        for (int i = threadIdx.x; i < s; i += blockDim.x)
+            if ((i & 1) == 0) load(i);
+        if (threadIdx.x == 0) x[s - 1] = xed;
+        __syncthreads();
+        const int ls = ilog2(s);
+        for (int p = ls - 1; p >= 0; p--) {  // src/tpr.cpp:277-308
+            const int u = 1 << p;
+            const int per = s / (2 * u);
+            for (int q = threadIdx.x; q < per; q += blockDim.x) {
+                const int i = u - 1 + 2 * u * q;
+                const T xu = i - u < 0 ? xprev : x[i - u];
+                x[i] = r[i] - a[i] * xu - c[i] * x[i + u];
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < s; i += blockDim.x) gx[i] = x[i];
 }
 
 // ---- sliced shape (large systems) ---------------------------------------
@@ -617,11 +831,61 @@ bool ref_needs_workspace(int kind, int n, int s, int prec) {
                              : !ref_uses_fused<double>(kind, n, s);
 }
 
+// One system per thread-block cluster of m = n / s CTAs (2 <= m <= 16),
+// one slice per CTA, EPT = s / threads rows per thread.
+template <typename T, int KIND, int EPT>
+static int launch_cluster_tpr(int nsys, int n, int s, const T *a, const T *diag,
+                              const T *c, const T *r, T *x, long long stride,
+                              cudaStream_t st) {
+    const int m = n / s;
+    const size_t smem = (7ULL * s + 10ULL * m + 3) * sizeof(T);
+    const int threads = std::min(refk::kThreads, std::max(32, s));
+    auto k = refk::cluster_tpr<T, KIND, EPT>;
+    static DeviceOnce set_to, nonportable;
+    int rc = smem_attr(k, smem, set_to);
+    if (rc) return rc;
+    int dev = 0;
+    TPRGB_CUDA(cudaGetDevice(&dev));
+    if (!nonportable.get(dev)) {
+        TPRGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+        nonportable.set(dev, 1);
+    }
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)m;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(nsys * m), 1, 1);
+    cfg.blockDim = dim3((unsigned)threads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    TPRGB_CUDA(cudaLaunchKernelEx(&cfg, k, a, diag, c, r, x, n, s, stride));
+    return TPRGB_OK;
+}
+
+template <typename T, int KIND>
+static int launch_cluster_ept(int nsys, int n, int s, const T *a, const T *diag, const T *c,
+                              const T *r, T *x, long long stride, cudaStream_t st) {
+    switch (std::max(1, s / refk::kThreads)) {
+        case 1: return launch_cluster_tpr<T, KIND, 1>(nsys, n, s, a, diag, c, r, x, stride, st);
+        case 2: return launch_cluster_tpr<T, KIND, 2>(nsys, n, s, a, diag, c, r, x, stride, st);
+        case 4: return launch_cluster_tpr<T, KIND, 4>(nsys, n, s, a, diag, c, r, x, stride, st);
+        default: return launch_cluster_tpr<T, KIND, 8>(nsys, n, s, a, diag, c, r, x, stride, st);
+    }
+}
+
 template <typename T, int KIND>
 static int launch_tpr_kind(int nsys, int n, int s, const T *a, const T *c,
                            const T *r, T *x, long long stride, T *work,
                            cudaStream_t st) {
     const int m = n / s;
+    if (ref_uses_fused<T>(KIND, n, s) && m >= 2 && m <= 16) {
+        // one slice per CTA of a thread-block cluster
+        return launch_cluster_ept<T, KIND>(nsys, n, s, a, nullptr, c, r, x, stride, st);
+    }
     if (ref_uses_fused<T>(KIND, n, s)) {
         size_t smem = (size_t)refk::fused_elems(n, s) * sizeof(T);
         int threads = std::min(refk::kThreads, std::max(64, n));
@@ -713,6 +977,41 @@ int launch_ref(int kind, int nsys, int n, int s, int prec, const void *a,
     return launch_ref_t<double>(kind, nsys, n, s, (const double *)a,
                                 (const double *)c, (const double *)r,
                                 (double *)x, stride, (double *)work, st);
+}
+
+// The one-launch path of a solver handle: one TPR / PTPR system on a
+// thread-block cluster (2 <= n / s <= 16 slices of the fused shape), inputs
+// (with the diagonal, or diag null) and output at device-accessible
+// addresses -- pinned host memory in the handle's case.
+bool ref_direct_ok(int kind, int n, int s, int prec) {
+    if (kind != TPRGB_PTPR && kind != TPRGB_TPR) return false;
+    if (n / s < 2 || n / s > 16) return false;
+    return prec == TPRGB_F32 ? ref_uses_fused<float>(kind, n, s)
+                             : ref_uses_fused<double>(kind, n, s);
+}
+
+int launch_ref_direct(int kind, int n, int s, int prec, const void *a, const void *diag,
+                      const void *c, const void *r, void *x, cudaStream_t st) {
+    if (!ref_direct_ok(kind, n, s, prec))
+        return fail(TPRGB_EUNSUPPORTED, "no one-launch path for n=%d, s=%d", n, s);
+    if (prec == TPRGB_F32) {
+        auto f = [&](auto kd) {
+            constexpr int K = decltype(kd)::value;
+            return launch_cluster_ept<float, K>(1, n, s, (const float *)a, (const float *)diag,
+                                                (const float *)c, (const float *)r,
+                                                (float *)x, n, st);
+        };
+        return kind == TPRGB_PTPR ? f(std::integral_constant<int, TPRGB_PTPR>())
+                                  : f(std::integral_constant<int, TPRGB_TPR>());
+    }
+    auto f = [&](auto kd) {
+        constexpr int K = decltype(kd)::value;
+        return launch_cluster_ept<double, K>(1, n, s, (const double *)a, (const double *)diag,
+                                             (const double *)c, (const double *)r,
+                                             (double *)x, n, st);
+    };
+    return kind == TPRGB_PTPR ? f(std::integral_constant<int, TPRGB_PTPR>())
+                              : f(std::integral_constant<int, TPRGB_TPR>());
 }
 
 int launch_normalize(int prec, long long neq, void *a, const void *diag,

@@ -73,7 +73,23 @@ def plain(iters=1000):
         dt = (time.perf_counter() - t0) / iters
         err = float(np.linalg.norm(x.astype(np.float64) - xt) /
                     np.linalg.norm(xt))
+        # the same round trip timed in C++ (no Python per call), with the
+        # 3-argument setter on the diag-normalised system (as tpr_pm
+        # sets it) and with the 4-argument setter on the raw one
+        L = T.load()
+        h = t._h
+        us3, us4 = ctypes.c_double(), ctypes.c_double()
+        an3, cn3, rn3 = (np.ascontiguousarray((v / b).astype(np.float32)) for v in (a, c, d))
+        xo = np.empty(2048, np.float32)
+        ptr = lambda v: v.ctypes.data_as(ctypes.c_void_p)
+        T.check(L.tprgb_time_roundtrip(h, ptr(an3), None, ptr(cn3), ptr(rn3), ptr(xo),
+                                       iters, ctypes.byref(us3)))
+        a4, b4, c4, d4 = (np.ascontiguousarray(v, np.float32) for v in (a, b, c, d))
+        T.check(L.tprgb_time_roundtrip(h, ptr(a4), ptr(b4), ptr(c4), ptr(d4), ptr(xo),
+                                       iters, ctypes.byref(us4)))
         out[name] = {"us_per_solve_host_round_trip": dt * 1e6,
+                     "us_per_solve_round_trip_cxx_3arg": us3.value,
+                     "us_per_solve_round_trip_cxx_4arg": us4.value,
                      "rel_l2_vs_xt": err}
     # device-only time of the fused kernel
     import torch
