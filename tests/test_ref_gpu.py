@@ -164,3 +164,29 @@ def test_invalid_arguments_return_codes(cuda):
     t = T.PTPR(64, 8)
     with pytest.raises(T.TprError):
         t.solve()  # no system set
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_timed_round_trip_same_bits(cuda, golden, prec):
+    """tprgb_time_roundtrip runs the handle's set / solve / get sequence in
+    C++ (4-argument setter): a positive time per round trip and the
+    reference's bits in x."""
+    import ctypes
+    dt = np.float32 if prec == "f32" else np.float64
+    L = T.load()
+    a, b, c, d = [np.ascontiguousarray(v, dt)
+                  for v in G.one_system(2048, 42, "dominant")[:4]]
+    p = lambda v: v.ctypes.data_as(ctypes.c_void_p)
+    for kind, key in ((T.PTPR_KIND, "ptpr"), (T.TPR_KIND, "tpr")):
+        h = ctypes.c_void_p()
+        T.check(L.tprgb_create(kind, 2048, 512, T.F32 if prec == "f32" else T.F64,
+                               ctypes.byref(h)))
+        try:
+            us = ctypes.c_double()
+            x = np.zeros(2048, dt)
+            T.check(L.tprgb_time_roundtrip(h, p(a), p(b), p(c), p(d), p(x), 5,
+                                           ctypes.byref(us)))
+            assert us.value > 0
+            _bits_equal(x, golden[f"plain_{key}_s512_{prec}"])
+        finally:
+            L.tprgb_destroy(h)
