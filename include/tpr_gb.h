@@ -172,7 +172,9 @@ TPRGB_API int tprgb_release_cached(void);
  * (src/ptpr.cu:542-600).
  * ====================================================================== */
 #define TPRGB_RESID_DF 0  /* residual in compensated FP32 (~2^-48)  */
-#define TPRGB_RESID_F64 1 /* residual in native FP64                */
+#define TPRGB_RESID_F64 1 /* residual in native FP64, x kept in FP64:
+                             cluster (variant 5), register (1) and queue
+                             kernels; the staged variants refuse it */
 
 typedef struct tprgb_batch_opts {
     int refine_steps;    /* 0: plain FP32 solve; k: k refinement steps      */
