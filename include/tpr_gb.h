@@ -235,6 +235,19 @@ TPRGB_API int tprgb_batch_solve_host(tprgb_host_ctx *ctx, int nsys, int n,
                                      const float *c, const float *d, void *x,
                                      const tprgb_batch_opts *opts);
 
+/* The same without waiting: the batch is queued behind the context's
+ * earlier work, so a stream of batches overlaps one batch's downloads with
+ * the next one's uploads instead of filling and draining the pipeline per
+ * call.  The host arrays must stay untouched, and x unread, until
+ * tprgb_host_ctx_wait returns.  No reference counterpart. */
+TPRGB_API int tprgb_batch_solve_host_async(tprgb_host_ctx *ctx, int nsys, int n,
+                                           const float *a, const float *b,
+                                           const float *c, const float *d,
+                                           void *x, const tprgb_batch_opts *opts);
+
+/* Waits until every batch queued on the context is solved and in its x. */
+TPRGB_API int tprgb_host_ctx_wait(tprgb_host_ctx *ctx);
+
 /* ---- tile table (filled by the autotuner, tpr_gb300/autotune.py) ------
  * Tile of the uniform kernel for systems of size n: equations per thread,
  * threads per CTA and variant (as in tprgb_batch_opts).  Also gives the equations per thread the

@@ -293,3 +293,22 @@ def test_host_pipeline_matches_device_solve(cuda, nsys, chunk_systems):
     x.zero_()
     ctx.solve(nsys, n, *views, x, B.opts(refine_steps=1))
     np.testing.assert_array_equal(x.numpy(), want)
+
+
+def test_host_pipeline_async_calls_pipeline_correctly(cuda):
+    """Asynchronous host calls queued back to back (different inputs,
+    different outputs, the ring shared across calls) give each batch the
+    device solve's bits once the context is waited on."""
+    bts = [G.uniform_batch(300, 1024, 70 + i, "dominant") for i in range(3)]
+    ctx = B.HostContext(chunk_eq=32 * 1024)
+    try:
+        o = B.opts(refine_steps=1)
+        outs = [np.empty(300 * 1024, np.float64) for _ in bts]
+        for bt, x in zip(bts, outs):
+            ctx.solve_async(300, 1024, bt.a, bt.b, bt.c, bt.d, x, o)
+        ctx.wait()
+        for bt, x in zip(bts, outs):
+            ref = B.solve_host(bt, refine_steps=1)
+            np.testing.assert_array_equal(x, ref)
+    finally:
+        ctx.close()

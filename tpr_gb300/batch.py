@@ -34,6 +34,9 @@ def _declare(L):
         "tprgb_host_ctx_destroy": (i, [vp]),
         "tprgb_batch_solve_host": (i, [vp, i, i, vp, vp, vp, vp, vp,
                                        C.POINTER(BatchOpts)]),
+        "tprgb_batch_solve_host_async": (i, [vp, i, i, vp, vp, vp, vp, vp,
+                                             C.POINTER(BatchOpts)]),
+        "tprgb_host_ctx_wait": (i, [vp]),
         "tprgb_diag_pair_to_double": (i, [C.c_int64, vp, vp, vp, vp]),
         "tprgb_tune_set": (i, [i, i, i, i]),
         "tprgb_tune_get": (i, [i, C.POINTER(i), C.POINTER(i), C.POINTER(i)]),
@@ -136,6 +139,18 @@ class HostContext:
         check(load().tprgb_batch_solve_host(self._h, nsys, n, ptr(a), ptr(b),
                                             ptr(c), ptr(d), ptr(x),
                                             C.byref(o or opts())))
+
+    def solve_async(self, nsys, n, a, b, c, d, x, o: BatchOpts | None = None):
+        """Queue the batch behind earlier ones without waiting; keep a..d
+        and x untouched until wait()."""
+        ptr = lambda v: C.c_void_p(v.ctypes.data if isinstance(v, np.ndarray)
+                                   else v.data_ptr())
+        check(load().tprgb_batch_solve_host_async(
+            self._h, nsys, n, ptr(a), ptr(b), ptr(c), ptr(d), ptr(x),
+            C.byref(o or opts())))
+
+    def wait(self):
+        check(load().tprgb_host_ctx_wait(self._h))
 
     def close(self):
         if self._h is not None and self._h.value:

@@ -165,6 +165,9 @@ struct tprgb_host_ctx {
     cudaEvent_t uploaded[kHostBufs] = {}, solved[kHostBufs] = {}, downloaded[kHostBufs] = {};
     float *d_in[kHostBufs] = {};  // a, b, c, d of one chunk
     void *d_x[kHostBufs] = {};    // x of one chunk (8 B / eq)
+    // chunks queued since creation: the ring position carries over from
+    // call to call, so asynchronous calls pipeline into each other
+    int64_t chunks = 0;
 };
 
 static void host_ctx_free(tprgb_host_ctx *h) {
@@ -222,10 +225,11 @@ TPRGB_API int tprgb_host_ctx_destroy(tprgb_host_ctx *h) {
     return TPRGB_OK;
 }
 
-TPRGB_API int tprgb_batch_solve_host(tprgb_host_ctx *h, int nsys, int n,
-                                     const float *a, const float *b,
-                                     const float *c, const float *d, void *x,
-                                     const tprgb_batch_opts *opts) {
+// Queues one batch on the context's three streams (upload, solve,
+// download) through its ring of device buffers, without waiting.
+static int host_enqueue(tprgb_host_ctx *h, int nsys, int n, const float *a,
+                        const float *b, const float *c, const float *d, void *x,
+                        const tprgb_batch_opts *opts) {
     if (!h) return fail(TPRGB_EINVAL, "ctx is NULL");
     if (nsys < 0 || n <= 0) return fail(TPRGB_EINVAL, "bad nsys/n");
     if (nsys == 0) return TPRGB_OK;
@@ -286,8 +290,9 @@ TPRGB_API int tprgb_batch_solve_host(tprgb_host_ctx *h, int nsys, int n,
                           (size_t)spacing <= h->max_pitch;
     int64_t s0 = 0;
     for (size_t ci = 0; ci < sizes.size(); ci++) {
-        const int k = (int)(ci % kHostBufs);
-        const bool reuse = ci >= (size_t)kHostBufs;  // buffer k held chunk ci - kHostBufs
+        const int64_t g = h->chunks++;  // the chunk's place in the ring
+        const int k = (int)(g % kHostBufs);
+        const bool reuse = g >= kHostBufs;  // buffer k held chunk g - kHostBufs
         const int64_t ns = sizes[ci];
         const int64_t off = s0 * n, neq = ns * n;
         float *da = h->d_in[k], *db = da + h->chunk_eq, *dc = db + h->chunk_eq,
@@ -328,13 +333,38 @@ TPRGB_API int tprgb_batch_solve_host(tprgb_host_ctx *h, int nsys, int n,
         if (e != cudaSuccess) return drained(cuda_fail(e, "tprgb_batch_solve_host"));
         s0 += ns;
     }
+    return TPRGB_OK;
+}
+
+static int host_wait(tprgb_host_ctx *h) {
     cudaError_t first = cudaSuccess;
     for (cudaStream_t s : {h->up, h->solve, h->down}) {
         const cudaError_t e = cudaStreamSynchronize(s);
         if (first == cudaSuccess) first = e;
     }
-    if (first != cudaSuccess) return cuda_fail(first, "tprgb_batch_solve_host");
+    if (first != cudaSuccess) return cuda_fail(first, "tprgb_host_ctx_wait");
     return TPRGB_OK;
+}
+
+TPRGB_API int tprgb_batch_solve_host(tprgb_host_ctx *h, int nsys, int n,
+                                     const float *a, const float *b,
+                                     const float *c, const float *d, void *x,
+                                     const tprgb_batch_opts *opts) {
+    int rc = host_enqueue(h, nsys, n, a, b, c, d, x, opts);
+    if (rc) return rc;
+    return host_wait(h);
+}
+
+TPRGB_API int tprgb_batch_solve_host_async(tprgb_host_ctx *h, int nsys, int n,
+                                           const float *a, const float *b,
+                                           const float *c, const float *d,
+                                           void *x, const tprgb_batch_opts *opts) {
+    return host_enqueue(h, nsys, n, a, b, c, d, x, opts);
+}
+
+TPRGB_API int tprgb_host_ctx_wait(tprgb_host_ctx *h) {
+    if (!h) return fail(TPRGB_EINVAL, "ctx is NULL");
+    return host_wait(h);
 }
 
 }  // extern "C"
