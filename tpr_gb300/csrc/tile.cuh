@@ -357,7 +357,44 @@ __device__ __forceinline__ void solve(const float (&a)[L], const float (&b)[L],
         __syncthreads();
         Row S0{0.f, 0.f, 0.f}, S1{0.f, 0.f, 0.f};
         const int q2 = lane & (W - 1);
-        if (!pc.on) {
+        if (!pc.on && W <= 4) {
+            // every lane solves the system's 2W segment rows (unit
+            // diagonal, in the order F_0, E_0, F_1, ...; outer couplings
+            // zero) itself by one elimination sweep and back-substitution
+            // from shared memory: no shuffles, no idle warps, no second
+            // barrier (the rows buffer is rewritten only after a later one)
+            constexpr int R = 2 * W;
+            float ra[R], rc[R], rd[R];
+#pragma unroll
+            for (int g = 0; g < W; g++) {
+                const SegRows sr = sm.rows[sys_warp0 + g];
+                ra[2 * g] = sr.R0.a;
+                rc[2 * g] = sr.R0.c;
+                rd[2 * g] = sr.R0.d;
+                ra[2 * g + 1] = sr.R1.a;
+                rc[2 * g + 1] = sr.R1.c;
+                rd[2 * g + 1] = sr.R1.d;
+            }
+#pragma unroll
+            for (int k = 1; k < R; k++) {
+                const float inv = hier::rcp(fmaf(-ra[k], rc[k - 1], 1.0f));
+                rc[k] *= inv;
+                rd[k] = fmaf(-ra[k], rd[k - 1], rd[k]) * inv;
+            }
+            float y[R];
+            y[R - 1] = rd[R - 1];
+#pragma unroll
+            for (int k = R - 2; k >= 0; k--) y[k] = fmaf(-rc[k], y[k + 1], rd[k]);
+            xf = y[0];
+            xl = y[1];
+#pragma unroll
+            for (int g = 1; g < W; g++) {
+                if (w == g) {
+                    xf = y[2 * g];
+                    xl = y[2 * g + 1];
+                }
+            }
+        } else if (!pc.on) {
             // every warp of the system solves the 2W segment rows itself:
             // no idle warps and no second barrier (the rows buffer is
             // rewritten only after a later barrier)
