@@ -863,50 +863,51 @@ __device__ __forceinline__ bool run_tile_smem(
                                    (float)xd[4 * i + 2], (float)xd[4 * i + 3]);
         }
         return finite;
-    }
-    float xlo[L];
-#pragma unroll
-    for (int i = 0; i < L; i++) xlo[i] = 0.f;
-    if (MODE == 1) {
-        for (int step = 0; step < refine_steps; step++) {
-            float hm, lm, hp, lp;
-            neighbours<NT, T>(xh[0], xh[L - 1], xlo[0], xlo[L - 1], t, hm, lm,
-                              hp, lp, sm, pc);
-            float r[L];
-            {
-                float a[L], b[L], c[L], d[L];
-                load4(a, b, c, d);
-                residuals<L>(a, b, c, d, xh, xlo, hm, lm, hp, lp, step > 0, r);
-            }
-            float dx[L];
-            {
-                float a[L], b[L], c[L], d[L];
-                load4(a, b, c, d);
-                if (step == refine_steps - 1) stage_free();
-                solve<L, NT, T, PP>(a, b, c, r, dx, sm, pc);
-            }
-#pragma unroll
-            for (int i = 0; i < L; i++) xlo[i] += dx[i];
-        }
-    }
-    bool finite = true;
-    if (!active) return true;
-    if (x_f64) {
-        finite = hier::store_pairs_f64<L>(xh, xlo, (double *)gx + base);
     } else {
-        float4 *o = reinterpret_cast<float4 *>((float *)gx + base);
+        float xlo[L];
 #pragma unroll
-        for (int i = 0; i < L / 4; i++) {
-            float v[4];
+        for (int i = 0; i < L; i++) xlo[i] = 0.f;
+        if (MODE == 1) {
+            for (int step = 0; step < refine_steps; step++) {
+                float hm, lm, hp, lp;
+                neighbours<NT, T>(xh[0], xh[L - 1], xlo[0], xlo[L - 1], t, hm, lm,
+                                  hp, lp, sm, pc);
+                float r[L];
+                {
+                    float a[L], b[L], c[L], d[L];
+                    load4(a, b, c, d);
+                    residuals<L>(a, b, c, d, xh, xlo, hm, lm, hp, lp, step > 0, r);
+                }
+                float dx[L];
+                {
+                    float a[L], b[L], c[L], d[L];
+                    load4(a, b, c, d);
+                    if (step == refine_steps - 1) stage_free();
+                    solve<L, NT, T, PP>(a, b, c, r, dx, sm, pc);
+                }
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                v[j] = xh[4 * i + j] + xlo[4 * i + j];
-                finite = finite && isfinite(v[j]);
+                for (int i = 0; i < L; i++) xlo[i] += dx[i];
             }
-            o[i] = make_float4(v[0], v[1], v[2], v[3]);
         }
+        bool finite = true;
+        if (!active) return true;
+        if (x_f64) {
+            finite = hier::store_pairs_f64<L>(xh, xlo, (double *)gx + base);
+        } else {
+            float4 *o = reinterpret_cast<float4 *>((float *)gx + base);
+#pragma unroll
+            for (int i = 0; i < L / 4; i++) {
+                float v[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    v[j] = xh[4 * i + j] + xlo[4 * i + j];
+                    finite = finite && isfinite(v[j]);
+                }
+                o[i] = make_float4(v[0], v[1], v[2], v[3]);
+            }
+        }
+        return finite;
     }
-    return finite;
 }
 
 }  // namespace tile
