@@ -71,7 +71,8 @@ TPRGB_API int tprgb_flops(int kind, int n, int s, int *flops);
  * ====================================================================== */
 
 /* Scratch bytes tprgb_ref_solve_device needs for `nsys` systems (0 when the
- * system fits one CTA's shared memory). */
+ * system fits one CTA's shared memory: CR / PCR up to n = 8192 in FP32 and
+ * 4096 in FP64; above, CR needs 3n and PCR 6n elements per system). */
 TPRGB_API int tprgb_ref_workspace_bytes(int kind, int nsys, int n, int s,
                                         int prec, size_t *bytes);
 
@@ -96,7 +97,8 @@ TPRGB_API int tprgb_ref_solve_device(int kind, int nsys, int n, int s,
  * that loads the library until exit).  The first call on a device (and
  * after a cudaDeviceReset) looks up the array's address, so make it before
  * any stream capture; workspace needs above 16 MiB (nsys * (3n + 3n/s)
- * elements) return TPRGB_EUNSUPPORTED; all calls share the array, so calls
+ * elements for TPR / PTPR, nsys * 3n for CR and 6n for PCR above one CTA)
+ * return TPRGB_EUNSUPPORTED; all calls share the array, so calls
  * that overlap on the GPU race. */
 TPRGB_API int tprgb_ref_solve_device_static(int kind, int nsys, int n, int s,
                                             int prec, const void *d_a,

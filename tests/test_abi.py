@@ -55,6 +55,15 @@ def test_error_paths_without_gpu(lib):
     assert lib.tprgb_ref_workspace_bytes(0, 2, 1 << 16, 256, 0, ctypes.byref(sz)) == 0
     assert sz.value == 2 * (3 * 65536 + 3 * 256) * 4
     assert lib.tprgb_ref_workspace_bytes(0, 1, 1024, 3, 0, ctypes.byref(sz)) == EINVAL
+    # standalone CR / PCR: none while n fits one CTA (8192 FP32, 4096 FP64),
+    # then one set of a, c, rhs per system for CR and two for PCR
+    for kind, prec, n, want in [(2, 0, 8192, 0), (3, 1, 4096, 0),
+                                (2, 1, 8192, 3 * 8192 * 8),
+                                (3, 0, 16384, 6 * 16384 * 4),
+                                (3, 1, 1 << 20, 6 * (1 << 20) * 8)]:
+        assert lib.tprgb_ref_workspace_bytes(kind, 2, n, 0, prec,
+                                             ctypes.byref(sz)) == 0
+        assert sz.value == 2 * want, (kind, prec, n)
     assert lib.tprgb_ref_solve_device(9, 1, 1024, 4, 0, None, None, None, None,
                                       None, 0, None) == EINVAL
     assert lib.tprgb_ref_solve_device(0, 1, 1024, 4, 0, None, None, None, None,

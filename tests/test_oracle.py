@@ -141,6 +141,21 @@ def test_reference_build_agrees_when_present(port):
 
 
 @pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_reference_cr_pcr_agree_at_large_n(port, prec):
+    """Standalone CR / PCR above one CTA's shared memory (n = 16384): the
+    port equals the compiled reference, which has no size cap."""
+    from oracle import oracle as O
+    r = O.ref(prec)
+    if r is None:
+        pytest.skip("reference solvers not built on this machine")
+    dt = np.float32 if prec == "f32" else np.float64
+    a, b, c, d, _ = G.one_system(16384, 9, "uneven")
+    an, cn, rn = port.normalize(a, b, c, d, dt)
+    np.testing.assert_array_equal(port.cr(an, cn, rn, dt)[0], r.cr(an, cn, rn)[0])
+    np.testing.assert_array_equal(port.pcr(an, cn, rn, dt)[0], r.pcr(an, cn, rn)[0])
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
 def test_timed_plain_loop_threads_same_bits(port, golden, prec):
     """The timed single-system loop with solver-internal OpenMP (stages 1
     and 3 parallel over slices) gives the fixtures' bits at any thread

@@ -56,6 +56,23 @@ def test_fixed_system_classes(cuda, golden, ans1024, prec):
 
 
 @pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_large_cr_pcr_objects(cuda, port, prec):
+    """CR / PCR objects and cr_cu / pcr_cu above one CTA's shared memory
+    (n = 32768, no size cap, as the reference's CPU classes): the handle
+    allocates the workspace; same bits as the C restatement."""
+    dt = np.float32 if prec == "f32" else np.float64
+    n = 1 << 15
+    a, b, c, d, _ = G.one_system(n, 5, "uneven")
+    an, cn, rn = port.normalize(a, b, c, d, dt)
+    _bits_equal(T.cr_cu(an, cn, rn, n, dt), port.cr(an, cn, rn, dt)[0])
+    _bits_equal(T.pcr_cu(an, cn, rn, n, dt), port.pcr(an, cn, rn, dt)[0])
+    t = T.PCR(n, dtype=dt)
+    t.set_tridiagonal_system(an, np.ones(n, dt), cn, rn)
+    assert t.solve() == 14 * n * 15  # src/pcr.cpp:88
+    _bits_equal(t.get_ans(), port.pcr(an, cn, rn, dt)[0])
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
 def test_fixed_system_free_functions(cuda, golden, ans1024, prec):
     dt = np.float32 if prec == "f32" else np.float64
     a, _, c, rhs = [v.astype(dt) for v in G.fixed_system(1024)]
@@ -116,14 +133,18 @@ def _device_batch(torch, nsys, n, dt, seed):
 @pytest.mark.parametrize("kind,n,s", [(0, 1024, 128), (1, 1024, 128),
                                       (0, 32768, 256), (1, 32768, 256),
                                       (0, 65536, 1024), (1, 16384, 64),
-                                      (2, 2048, 0), (3, 2048, 0)])
+                                      (2, 2048, 0), (3, 2048, 0),
+                                      (2, 8192, 0), (3, 8192, 0),
+                                      (2, 65536, 0), (3, 65536, 0)])
 def test_device_batched_vs_port(cuda, port, prec, kind, n, s):
     """Several systems per launch, fused and sliced shapes, against the C
-    restatement (bit for bit)."""
+    restatement (bit for bit).  Standalone CR / PCR run in one CTA's
+    shared memory up to n = 8192 (FP32) / 4096 (FP64) and level by level
+    over a global workspace above: 8192 covers both sides of the FP64
+    switch, 65536 the multi-launch CR levels (two before and after the
+    one-CTA tail)."""
     torch = cuda
     dt = np.float32 if prec == "f32" else np.float64
-    if prec == "f64" and kind >= 2 and n > 4096:
-        pytest.skip("outside the FP64 standalone CR/PCR limit")
     nsys = 3
     bt, norm, (da, dc, dr) = _device_batch(torch, nsys, n, dt, 100 + n)
     dx = torch.empty_like(da)

@@ -9,7 +9,8 @@ so the second call runs over the first call's leftovers in the shared
 array) and compares it with the existing entry point (caller-provided
 workspace) bit for bit -- the tolerance of the reference-semantics tests.
 Shapes: the sliced path (which uses the array), including the largest batch
-whose workspace fits in 16 MiB; the one-CTA fused path and standalone
+whose workspace fits in 16 MiB; standalone CR / PCR above one CTA's shared
+memory (which use it too); the one-CTA fused path and small standalone
 CR / PCR (which need no workspace); and one system past the limit.
 
 The file name sorts last so that a run stopping at its first failure has
@@ -90,6 +91,15 @@ def test_sliced_path_matches_caller_workspace(cuda, kind, prec):
 def test_paths_without_workspace_match(cuda, kind, n, s):
     assert _need(T.load(), kind, 4, n, s, T.F32) == 0
     _two_calls(cuda, kind, 4, n, s, T.F32, 21)
+
+
+@pytest.mark.parametrize("kind", [T.CR_KIND, T.PCR_KIND])
+def test_stepped_cr_pcr_uses_the_array(cuda, kind):
+    """Standalone CR / PCR above one CTA's shared memory keep their rows in
+    the workspace: 3 x 16384 FP64 systems (PCR: 2.4 MB of the array)."""
+    n, nsys = 1 << 14, 3
+    assert _need(T.load(), kind, nsys, n, n, T.F64) > 0
+    _two_calls(cuda, kind, nsys, n, n, T.F64, 41)
 
 
 def test_largest_batch_that_fits(cuda):

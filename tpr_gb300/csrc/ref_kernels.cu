@@ -232,6 +232,66 @@ __device__ __forceinline__ void inter_eq(T ak, T ck, T rk, T akr, T ckr,
     sr = inv * (rk - rkr * ck);
 }
 
+// Row k of one PCR step at distance s over m rows (src/pcr.cpp:30-75):
+// reads rows k - s, k, k + s of the previous step.
+template <typename T>
+__device__ __forceinline__ void pcr_row(const T *a, const T *c, const T *r,
+                                        int k, int m, int s, T &na, T &nc,
+                                        T &nr) {
+    if (k < s) {
+        int kr = k + s;
+        T ee = T(1) / (T(1) - c[k] * a[kr]);
+        na = ee * a[k];
+        nc = -ee * c[k] * c[kr];
+        nr = ee * (r[k] - c[k] * r[kr]);
+    } else if (k < m - s) {
+        int kl = k - s, kr = k + s;
+        T ap = a[k], cp = c[k];
+        T ee = T(1) / (T(1) - ap * c[kl] - cp * a[kr]);
+        na = -ee * ap * a[kl];
+        nc = -ee * cp * c[kr];
+        nr = ee * (r[k] - ap * r[kl] - cp * r[kr]);
+    } else {
+        int kl = k - s;
+        T ap = a[k], cp = c[k];
+        T ee = T(1) / (T(1) - ap * c[kl]);
+        na = -ee * ap * a[kl];
+        nc = ee * cp;
+        nr = ee * (r[k] - ap * r[kl]);
+    }
+}
+
+// Row i of CR forward level p (u = 2^p; src/cr.cpp:48-69): reads rows
+// i - u, i, i + u.
+template <typename T>
+__device__ __forceinline__ void cr_row(const T *a, const T *c, const T *r,
+                                       int i, int u, int m, T &na, T &nc,
+                                       T &nr) {
+    if (i < m - 2 * u)
+        upd_mid(a, c, r, i - u, i, i + u, na, nc, nr);
+    else
+        upd_lower(a, c, r, i - u, i, na, nc, nr);
+}
+
+// The last two rows of CR, m >= 2 (src/cr.cpp:89-96).
+template <typename T>
+__device__ __forceinline__ void cr_top(const T *a, const T *c, const T *r,
+                                       T *x, int m) {
+    const int i = m / 2 - 1, u = m / 2;
+    T inv_det = T(1) / (T(1) - c[i] * a[i + u]);
+    x[i] = (r[i] - c[i] * r[i + u]) * inv_det;
+    x[i + u] = (r[i + u] - r[i] * a[i + u]) * inv_det;
+}
+
+// Row i of CR back substitution at distance u, i < m - u
+// (src/cr.cpp:98-112).
+template <typename T>
+__device__ __forceinline__ T cr_back_row(const T *a, const T *c, const T *r,
+                                         const T *x, int i, int u) {
+    if (i == u - 1) return r[i] - c[i] * x[i + u];
+    return r[i] - a[i] * x[i - u] - c[i] * x[i + u];
+}
+
 // PCR on m rows in shared memory (src/pcr.cpp:15-89); rhs holds x on exit.
 template <typename T, int EPT = kEpt>
 __device__ void cta_pcr(T *a, T *c, T *r, int m) {
@@ -242,29 +302,7 @@ __device__ void cta_pcr(T *a, T *c, T *r, int m) {
 #pragma unroll
         for (int e = 0; e < EPT; e++) {
             int k = threadIdx.x + e * blockDim.x;
-            if (k < m) {
-                if (k < s) {
-                    int kr = k + s;
-                    T ee = T(1) / (T(1) - c[k] * a[kr]);
-                    na[e] = ee * a[k];
-                    nc[e] = -ee * c[k] * c[kr];
-                    nr[e] = ee * (r[k] - c[k] * r[kr]);
-                } else if (k < m - s) {
-                    int kl = k - s, kr = k + s;
-                    T ap = a[k], cp = c[k];
-                    T ee = T(1) / (T(1) - ap * c[kl] - cp * a[kr]);
-                    na[e] = -ee * ap * a[kl];
-                    nc[e] = -ee * cp * c[kr];
-                    nr[e] = ee * (r[k] - ap * r[kl] - cp * r[kr]);
-                } else {
-                    int kl = k - s;
-                    T ap = a[k], cp = c[k];
-                    T ee = T(1) / (T(1) - ap * c[kl]);
-                    na[e] = -ee * ap * a[kl];
-                    nc[e] = ee * cp;
-                    nr[e] = ee * (r[k] - ap * r[kl]);
-                }
-            }
+            if (k < m) pcr_row<T>(a, c, r, k, m, s, na[e], nc[e], nr[e]);
         }
         __syncthreads();
 #pragma unroll
@@ -296,13 +334,8 @@ __device__ void cta_cr(T *a, T *c, T *r, T *x, int m) {
 #pragma unroll
         for (int e = 0; e < EPT; e++) {
             int j = threadIdx.x + e * blockDim.x;
-            if (j < rows) {
-                int i = ux - 1 + ux * j;
-                if (i < m - ux)
-                    upd_mid(a, c, r, i - u, i, i + u, na[e], nc[e], nr[e]);
-                else
-                    upd_lower(a, c, r, i - u, i, na[e], nc[e], nr[e]);
-            }
+            if (j < rows)
+                cr_row<T>(a, c, r, ux - 1 + ux * j, u, m, na[e], nc[e], nr[e]);
         }
         __syncthreads();
 #pragma unroll
@@ -317,22 +350,14 @@ __device__ void cta_cr(T *a, T *c, T *r, T *x, int m) {
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        int i = m / 2 - 1, u = m / 2;
-        T inv_det = T(1) / (T(1) - c[i] * a[i + u]);
-        x[i] = (r[i] - c[i] * r[i + u]) * inv_det;
-        x[i + u] = (r[i + u] - r[i] * a[i + u]) * inv_det;
-    }
+    if (threadIdx.x == 0) cr_top<T>(a, c, r, x, m);
     __syncthreads();
     for (int k = ln - 2; k >= 0; k--) {
         const int u = 1 << k;
         const int rows = m / (2 * u);  // rows u-1 + 2u*j
         for (int j = threadIdx.x; j < rows; j += blockDim.x) {
-            int i = u - 1 + 2 * u * j;
-            if (j == 0)
-                x[i] = r[i] - c[i] * x[i + u];
-            else if (i < m - u)
-                x[i] = r[i] - a[i] * x[i - u] - c[i] * x[i + u];
+            const int i = u - 1 + 2 * u * j;  // i < m - u for every j
+            x[i] = cr_back_row<T>(a, c, r, x, i, u);
         }
         __syncthreads();
     }
@@ -473,6 +498,132 @@ fused_crpcr(const T *__restrict__ ga, const T *__restrict__ gc,
     } else {
         cta_cr(a, c, r, x, n);
         for (int i = threadIdx.x; i < n; i += blockDim.x) gx[base + i] = x[i];
+    }
+}
+
+// ---- standalone CR / PCR on systems larger than one CTA's shared memory ----
+// The rows live in a global workspace (L2-resident at these sizes) and each
+// level is one launch over all rows of all systems (blockIdx.y = system), or
+// -- for CR's levels of at most kThreads rows -- one CTA per system runs them
+// back to back.  Same per-row arithmetic as the shared-memory kernels.
+
+// One PCR step at distance s: reads the previous step's rows (the inputs at
+// s = 1), writes this step's; the last step writes only x (into orr).
+template <typename T>
+__global__ void __launch_bounds__(256)
+pcr_step(const T *__restrict__ ia, const T *__restrict__ ic,
+         const T *__restrict__ ir, long long istride, T *__restrict__ oa,
+         T *__restrict__ oc, T *__restrict__ orr, long long ostride, int m,
+         int s, int last) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m) return;
+    const long long ib = blockIdx.y * istride, ob = blockIdx.y * ostride;
+    T na, nc, nr;
+    pcr_row<T>(ia + ib, ic + ib, ir + ib, k, m, s, na, nc, nr);
+    if (!last) {
+        oa[ob + k] = na;
+        oc[ob + k] = nc;
+    }
+    orr[ob + k] = nr;
+}
+
+// CR forward level 0 from the inputs into the workspace w (stride
+// wstride): odd rows reduced, even rows copied, so that w holds every row
+// the later levels and the back substitution read.
+template <typename T>
+__global__ void __launch_bounds__(256)
+cr_first(const T *__restrict__ ga, const T *__restrict__ gc,
+         const T *__restrict__ gr, long long stride, T *__restrict__ wa,
+         T *__restrict__ wc, T *__restrict__ wr, long long wstride, int m) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m / 2) return;
+    const long long gb = blockIdx.y * stride, wb = blockIdx.y * wstride;
+    ga += gb;
+    gc += gb;
+    gr += gb;
+    wa += wb;
+    wc += wb;
+    wr += wb;
+    const int i = 2 * j + 1;
+    T na, nc, nr;
+    cr_row<T>(ga, gc, gr, i, 1, m, na, nc, nr);
+    wa[i - 1] = ga[i - 1];
+    wc[i - 1] = gc[i - 1];
+    wr[i - 1] = gr[i - 1];
+    wa[i] = na;
+    wc[i] = nc;
+    wr[i] = nr;
+}
+
+// CR forward level p >= 1 in place: row i = 2u - 1 + 2u j reads rows i +- u,
+// which this level does not write, so no row is read after another thread
+// wrote it.
+template <typename T>
+__global__ void __launch_bounds__(256)
+cr_forward(T *wa, T *wc, T *wr, long long wstride, int m, int p) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int u = 1 << p;
+    if (j >= (m >> (p + 1))) return;
+    const long long wb = blockIdx.y * wstride;
+    const int i = 2 * u - 1 + 2 * u * j;
+    T na, nc, nr;
+    cr_row<T>(wa + wb, wc + wb, wr + wb, i, u, m, na, nc, nr);
+    wa[wb + i] = na;
+    wc[wb + i] = nc;
+    wr[wb + i] = nr;
+}
+
+// CR back substitution at distance u = 2^k into x (stride xstride).
+template <typename T>
+__global__ void __launch_bounds__(256)
+cr_backward(const T *wa, const T *wc, const T *wr, long long wstride, T *gx,
+            long long xstride, int m, int k) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int u = 1 << k;
+    if (j >= (m >> (k + 1))) return;
+    const long long wb = blockIdx.y * wstride;
+    const int i = u - 1 + 2 * u * j;
+    T *x = gx + blockIdx.y * xstride;
+    x[i] = cr_back_row<T>(wa + wb, wc + wb, wr + wb, x, i, u);
+}
+
+// CR levels p0 .. log2(m) - 2 forward, the last two rows, and back
+// substitution down to level p0, on one CTA per system: every level of
+// these has at most blockDim.x rows.  Global writes of one level are
+// visible to the block's other threads after the barrier.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+cr_tail(T *wa, T *wc, T *wr, long long wstride, T *gx, long long xstride,
+        int m, int p0) {
+    const long long wb = blockIdx.x * wstride;
+    wa += wb;
+    wc += wb;
+    wr += wb;
+    T *x = gx + blockIdx.x * xstride;
+    const int ln = ilog2(m);
+    for (int p = p0; p < ln - 1; p++) {
+        const int u = 1 << p;
+        const int j = threadIdx.x;
+        if (j < (m >> (p + 1))) {
+            const int i = 2 * u - 1 + 2 * u * j;
+            T na, nc, nr;
+            cr_row<T>(wa, wc, wr, i, u, m, na, nc, nr);
+            wa[i] = na;
+            wc[i] = nc;
+            wr[i] = nr;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) cr_top<T>(wa, wc, wr, x, m);
+    __syncthreads();
+    for (int k = ln - 2; k >= p0; k--) {
+        const int u = 1 << k;
+        const int j = threadIdx.x;
+        if (j < (m >> (k + 1))) {
+            const int i = u - 1 + 2 * u * j;
+            x[i] = cr_back_row<T>(wa, wc, wr, x, i, u);
+        }
+        __syncthreads();
     }
 }
 
@@ -783,7 +934,8 @@ static int smem_attr(K k, size_t smem, DeviceOnce &set_to) {
 template <typename T>
 static bool ref_uses_fused(int kind, int n, int s) {
     if (kind == TPRGB_CR || kind == TPRGB_PCR)
-        return true;
+        return 4LL * n * (long long)sizeof(T) <= (long long)kFusedSmemLimit &&
+               n <= refk::kThreads * refk::kEpt;
     return refk::fused_elems(n, s) * (long long)sizeof(T) <=
                (long long)kFusedSmemLimit &&
            n <= refk::kThreads * refk::kEpt;
@@ -797,13 +949,7 @@ int ref_validate(int kind, int n, int s, int prec) {
     if (!is_pow2(n))
         return fail(TPRGB_EINVAL, "n=%d must be a power of two", n);
     const size_t esz = prec == TPRGB_F32 ? 4 : 8;
-    if (kind == TPRGB_CR || kind == TPRGB_PCR) {
-        if ((size_t)n * 4 * esz > kFusedSmemLimit || n > refk::kThreads * refk::kEpt)
-            return fail(TPRGB_EUNSUPPORTED,
-                        "standalone CR/PCR supports n <= %zu here (n=%d)",
-                        kFusedSmemLimit / (4 * esz), n);
-        return TPRGB_OK;
-    }
+    if (kind == TPRGB_CR || kind == TPRGB_PCR) return TPRGB_OK;
     if (!is_pow2(s) || s < 2 || s > n)
         return fail(TPRGB_EINVAL,
                     "s=%d must be a power of two with 2 <= s <= n=%d", s, n);
@@ -821,12 +967,13 @@ int ref_validate(int kind, int n, int s, int prec) {
 }
 
 size_t ref_workspace_elems(int kind, int n, int s) {
-    if (kind == TPRGB_CR || kind == TPRGB_PCR) return 0;
+    if (kind == TPRGB_PCR) return 6ULL * n;
+    if (kind == TPRGB_CR) return 3ULL * n;
     return 3ULL * n + 3ULL * (n / s);
 }
 
 bool ref_needs_workspace(int kind, int n, int s, int prec) {
-    if (kind == TPRGB_CR || kind == TPRGB_PCR) return false;
+    if (kind == TPRGB_CR || kind == TPRGB_PCR) s = n;
     return prec == TPRGB_F32 ? !ref_uses_fused<float>(kind, n, s)
                              : !ref_uses_fused<double>(kind, n, s);
 }
@@ -941,6 +1088,58 @@ static int launch_tpr_kind(int nsys, int n, int s, const T *a, const T *c,
     return TPRGB_OK;
 }
 
+// Standalone CR / PCR of more rows than one CTA's shared memory holds: one
+// launch per level over the workspace (PCR: two sets of a, c, rhs per
+// system, written alternately; CR: one set, reduced in place), CR's levels
+// of at most kThreads rows on one CTA per system.
+template <typename T>
+static int launch_crpcr_stepped(int kind, int nsys, int n, const T *a,
+                                const T *c, const T *r, T *x, long long stride,
+                                T *work, cudaStream_t st) {
+    if (work == nullptr)
+        return fail(TPRGB_EINVAL, "standalone %s of n=%d needs a workspace",
+                    kind == TPRGB_CR ? "CR" : "PCR", n);
+    int ln = 0;
+    while ((1 << ln) < n) ln++;
+    const long long ws = (long long)ref_workspace_elems(kind, n, n);
+    constexpr int kB = 256;
+    if (kind == TPRGB_PCR) {
+        for (int p = 0; p < ln; p++) {
+            const T *set_in = work + ((p - 1) & 1) * 3LL * n;
+            T *set_out = work + (p & 1) * 3LL * n;
+            const bool first = p == 0, last = p == ln - 1;
+            refk::pcr_step<T><<<dim3(n / kB, nsys), kB, 0, st>>>(
+                first ? a : set_in, first ? c : set_in + n,
+                first ? r : set_in + 2LL * n, first ? stride : ws,
+                last ? x : set_out, last ? x : set_out + n,
+                last ? x : set_out + 2LL * n, last ? stride : ws, n, 1 << p,
+                last ? 1 : 0);
+            TPRGB_CUDA(cudaGetLastError());
+        }
+        return TPRGB_OK;
+    }
+    T *wa = work, *wc = work + n, *wr = work + 2LL * n;
+    int p0 = 1;  // first level of at most kThreads rows
+    while ((n >> (p0 + 1)) > refk::kThreads) p0++;
+    refk::cr_first<T><<<dim3(n / 2 / kB, nsys), kB, 0, st>>>(a, c, r, stride, wa,
+                                                             wc, wr, ws, n);
+    TPRGB_CUDA(cudaGetLastError());
+    for (int p = 1; p < p0; p++) {
+        refk::cr_forward<T><<<dim3((n >> (p + 1)) / kB, nsys), kB, 0, st>>>(
+            wa, wc, wr, ws, n, p);
+        TPRGB_CUDA(cudaGetLastError());
+    }
+    refk::cr_tail<T><<<nsys, refk::kThreads, 0, st>>>(wa, wc, wr, ws, x, stride,
+                                                       n, p0);
+    TPRGB_CUDA(cudaGetLastError());
+    for (int k = p0 - 1; k >= 0; k--) {
+        refk::cr_backward<T><<<dim3((n >> (k + 1)) / kB, nsys), kB, 0, st>>>(
+            wa, wc, wr, ws, x, stride, n, k);
+        TPRGB_CUDA(cudaGetLastError());
+    }
+    return TPRGB_OK;
+}
+
 template <typename T>
 static int launch_ref_t(int kind, int nsys, int n, int s, const T *a,
                         const T *c, const T *r, T *x, long long stride,
@@ -953,6 +1152,9 @@ static int launch_ref_t(int kind, int nsys, int n, int s, const T *a,
             return launch_tpr_kind<T, TPRGB_TPR>(nsys, n, s, a, c, r, x,
                                                  stride, work, st);
         default: {
+            if (!ref_uses_fused<T>(kind, n, n))
+                return launch_crpcr_stepped<T>(kind, nsys, n, a, c, r, x,
+                                               stride, work, st);
             size_t smem = 4ULL * n * sizeof(T);
             int threads = std::min(refk::kThreads, std::max(64, n));
             auto k = kind == TPRGB_CR ? refk::fused_crpcr<T, TPRGB_CR>
@@ -1123,7 +1325,7 @@ static int static_work_ptr(void **out) {
 // another driver context) looks up the array's device address with
 // cudaGetSymbolAddress; make that first call before any stream capture.
 // Systems whose workspace exceeds 16 MiB in total (nsys * (3n + 3n/s)
-// elements) are rejected with TPRGB_EUNSUPPORTED.  All calls share the
+// elements for TPR / PTPR, nsys * 3n for CR and 6n for PCR) are rejected with TPRGB_EUNSUPPORTED.  All calls share the
 // array and it keeps the last call's contents (no part of it needs to
 // start at zero: every workspace element is written before it is read), so
 // calls that overlap on the GPU -- on different streams, or from different
