@@ -40,11 +40,10 @@ CANDIDATES = [(4, 128, 1), (4, 256, 1), (4, 512, 1), (4, 1024, 1),
               (8, 128, 4), (16, 64, 4), (16, 128, 4), (16, 256, 4),
               (16, 64, 5), (16, 128, 5), (16, 256, 5)]
 # Cluster CTAs of 512 threads (one per SM: 132 KB of staging) serve
-# n = 16384 .. 65536 when asked for explicitly.  Alone they time 5 % faster
-# than 256 threads at n = 65536 (0.213 vs 0.225 ms per 16.8 M equations), but
-# in a mixed-size plan, whose size groups run side by side, they took the
-# 4096-system uneven batch from 7.85 M to 6.85 M systems/s, so the uniform
-# timings here would mislead the table and they are not candidates.
+# n = 16384 .. 65536 when asked for explicitly.  They time 10-14 % slower
+# than 256 threads alone (n = 65536: 0.195 vs 0.176 ms per 16.8 M equations;
+# 32768: 0.158 vs 0.138) and, routed for n = 65536 in the 4096-system uneven
+# plan, 7.7 M against 9.25 M systems/s, so they are not candidates.
 VARIANT_TAG = {1: "", 2: "s", 3: "w", 4: "w1", 5: "c"}
 
 
