@@ -175,6 +175,62 @@ def test_device_batched_vs_port(cuda, port, prec, kind, n, s):
         _bits_equal(x[sl], xr)
 
 
+EDGE_SHAPES = [(2, 2), (4, 2), (8, 2), (8, 8), (16, 2), (32, 2), (64, 2),
+               (64, 4), (1024, 2), (4096, 2), (32768, 4), (65536, 8)]
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+@pytest.mark.parametrize("kind", [0, 1])
+def test_edge_shapes_vs_port(cuda, port, prec, kind):
+    """The smallest slices and systems (s = 2, n = s, n = 2), one-launch
+    cluster shapes (2 <= n / s <= 16), one-CTA shapes with a long reduced
+    system (m = 512 at s = 2), and the sliced path at its largest reduced
+    system (m = 8192, which FP64 rejects as more than one CTA's shared
+    memory): same bits as the C restatement, through the batched device
+    entry point and through the *_cu host functions."""
+    torch = cuda
+    dt = np.float32 if prec == "f32" else np.float64
+    L = T.load()
+    pr = T.F32 if prec == "f32" else T.F64
+    cu = T.ptpr_cu if kind == 0 else T.tpr_cu
+    for n, s in EDGE_SHAPES:
+        nsys = 2
+        bt, norm, (da, dc, dr) = _device_batch(torch, nsys, n, dt, 300 + n + s)
+        sz = ctypes.c_size_t()
+        rc = L.tprgb_ref_workspace_bytes(kind, nsys, n, s, pr, ctypes.byref(sz))
+        if rc == T.EUNSUPPORTED:
+            assert prec == "f64" and n // s == 8192, (n, s)
+            continue
+        T.check(rc)
+        work = torch.empty(max(1, sz.value), dtype=torch.uint8, device="cuda")
+        dx = torch.empty_like(da)
+        T.check(L.tprgb_ref_solve_device(
+            kind, nsys, n, s, pr, da.data_ptr(), dc.data_ptr(), dr.data_ptr(),
+            dx.data_ptr(), work.data_ptr() if sz.value else None, sz.value,
+            torch.cuda.current_stream().cuda_stream))
+        torch.cuda.synchronize()
+        x = dx.cpu().numpy()
+        for k in range(nsys):
+            sl = slice(k * n, (k + 1) * n)
+            a, c, r = norm[0][sl], norm[1][sl], norm[2][sl]
+            xr = (port.ptpr if kind == 0 else port.tpr)(a, c, r, s, dt)[0]
+            _bits_equal(x[sl], xr)
+            if k == 0:
+                _bits_equal(cu(a, c, r, n, s, dt), xr)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_tiny_cr_pcr_vs_port(cuda, port, prec):
+    """Standalone CR / PCR on n = 1, 2, 4, 8 (n = 1: x = rhs, no reduction;
+    n = 2: the two-row solve alone): same bits as the C restatement."""
+    dt = np.float32 if prec == "f32" else np.float64
+    for n in (1, 2, 4, 8):
+        a, b, c, d, _ = G.one_system(max(n, 2), 17 + n, "uneven")
+        an, cn, rn = port.normalize(a[:n], b[:n], c[:n], d[:n], dt)
+        _bits_equal(T.cr_cu(an, cn, rn, n, dt), port.cr(an, cn, rn, dt)[0])
+        _bits_equal(T.pcr_cu(an, cn, rn, n, dt), port.pcr(an, cn, rn, dt)[0])
+
+
 def test_invalid_arguments_return_codes(cuda):
     with pytest.raises(T.TprError) as e:
         T.PTPR(1000, 8)
