@@ -40,7 +40,8 @@ int launch_normalize(int prec, long long neq, void *a, const void *diag,
                      void *c, void *r, cudaStream_t st);
 bool ref_direct_ok(int kind, int n, int s, int prec);
 int launch_ref_direct(int kind, int n, int s, int prec, const void *a, const void *diag,
-                      const void *c, const void *r, void *x, cudaStream_t st);
+                      const void *c, const void *r, void *x, unsigned *done,
+                      cudaStream_t st);
 
 static int flops_of(int kind, int n, int s) {
     int ln = ilog2(n);
@@ -85,7 +86,38 @@ struct tprgb_solver {
     // normalising launch).  Other shapes upload, normalise and download.
     bool direct = false;
     bool use_diag = false;
+    // One-launch path on a GPU with native atomics on host memory: the
+    // kernel's CTAs count a mapped word up as their part of x lands, and the
+    // handle waits for it by reading host memory (done / expect / seen:
+    // counts enqueued and confirmed) instead of a driver synchronisation.
+    unsigned *h_done = nullptr, *hd_done = nullptr;
+    unsigned expect = 0, seen = 0;
 };
+
+// Waits until every enqueued one-launch solve has written x (and so has
+// read the staging): polls the completion word for up to ~200 us, then
+// falls back to a stream synchronisation, which also reports a failed
+// launch.
+static int wait_direct(tprgb_solver *h) {
+    if (h->seen == h->expect) return TPRGB_OK;
+    if (h->h_done) {
+        const auto t0 = std::chrono::steady_clock::now();
+        for (unsigned i = 1;; i++) {
+            if (__atomic_load_n(h->h_done, __ATOMIC_ACQUIRE) == h->expect) {
+                h->seen = h->expect;
+                return TPRGB_OK;
+            }
+            if ((i & 255u) == 0 && std::chrono::steady_clock::now() - t0 >
+                                       std::chrono::microseconds(200))
+                break;
+        }
+    }
+    TPRGB_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->h_done && __atomic_load_n(h->h_done, __ATOMIC_ACQUIRE) != h->expect)
+        return fail(TPRGB_ECUDA, "one-launch solve ended without counting its parts");
+    h->seen = h->expect;
+    return TPRGB_OK;
+}
 
 extern "C" {
 
@@ -156,6 +188,7 @@ static void free_handle(tprgb_solver *h) {
     if (!h) return;
     if (h->staged) cudaEventDestroy(h->staged);
     cudaFreeHost(h->h_stage);
+    if (h->h_done) cudaFreeHost(h->h_done);
     cudaFree(h->d_a);
     cudaFree(h->d_work);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -197,6 +230,23 @@ TPRGB_API int tprgb_create(int kind, int n, int s, int prec,
     }
     h->h_x = h->h_stage + 4 * (size_t)n * h->esz;
     h->direct = ref_direct_ok(kind, n, s, prec);
+    if (h->direct) {
+        int dev = 0, native = 0;
+        e = cudaGetDevice(&dev);
+        if (e == cudaSuccess)
+            e = cudaDeviceGetAttribute(&native, cudaDevAttrHostNativeAtomicSupported, dev);
+        if (e == cudaSuccess && native) {
+            e = cudaHostAlloc((void **)&h->h_done, 64, cudaHostAllocMapped);
+            if (e == cudaSuccess) {
+                *h->h_done = 0;
+                e = cudaHostGetDevicePointer((void **)&h->hd_done, h->h_done, 0);
+            }
+        }
+        if (e != cudaSuccess) {
+            free_handle(h);
+            return cuda_fail(e, "completion word");
+        }
+    }
     char *p = (char *)h->d_a;
     h->d_c = p + 1 * (size_t)n * h->esz;
     h->d_r = p + 2 * (size_t)n * h->esz;
@@ -226,8 +276,13 @@ TPRGB_API int tprgb_set_system(tprgb_solver *h, const void *a,
     if (!h) return fail(TPRGB_EINVAL, "handle is NULL");
     if (!a || !c || !rhs) return fail(TPRGB_EINVAL, "null host array");
     const size_t bytes = (size_t)h->n * h->esz;
-    // the previous upload must have left the staging buffer
-    TPRGB_CUDA(cudaEventSynchronize(h->staged));
+    // the previous upload (or one-launch solve) must have left the staging
+    if (h->direct) {
+        int rc = wait_direct(h);
+        if (rc) return rc;
+    } else {
+        TPRGB_CUDA(cudaEventSynchronize(h->staged));
+    }
     // CR ignores diag as the reference's setter does (src/cr.cpp:17-21)
     const bool use_diag = diag && h->kind != TPRGB_CR;
     memcpy(h->h_stage, a, bytes);
@@ -263,10 +318,10 @@ TPRGB_API int tprgb_solve(tprgb_solver *h, int *flops) {
         rc = launch_ref_direct(h->kind, h->n, h->s, h->prec, h->hd_stage,
                                h->use_diag ? h->hd_stage + 3 * bytes : nullptr,
                                h->hd_stage + bytes, h->hd_stage + 2 * bytes,
-                               h->hd_stage + 4 * bytes, h->stream);
+                               h->hd_stage + 4 * bytes, h->hd_done, h->stream);
         if (rc) return rc;
-        // the next set_system waits until this solve has read the staging
-        TPRGB_CUDA(cudaEventRecord(h->staged, h->stream));
+        // the next set_system / get_ans waits for this solve's parts
+        h->expect += (unsigned)(h->n / h->s);
     } else {
         rc = launch_ref(h->kind, 1, h->n, h->s, h->prec, h->d_a, h->d_c,
                         h->d_r, h->d_x, h->n, h->d_work, h->stream);
@@ -280,10 +335,14 @@ TPRGB_API int tprgb_get_ans(tprgb_solver *h, void *x) {
     if (!h) return fail(TPRGB_EINVAL, "handle is NULL");
     if (!x) return fail(TPRGB_EINVAL, "x is NULL");
     const size_t bytes = (size_t)h->n * h->esz;
-    if (!h->direct)
+    if (h->direct) {
+        int rc = wait_direct(h);
+        if (rc) return rc;
+    } else {
         TPRGB_CUDA(cudaMemcpyAsync(h->h_x, h->d_x, bytes, cudaMemcpyDeviceToHost,
                                    h->stream));
-    TPRGB_CUDA(cudaStreamSynchronize(h->stream));
+        TPRGB_CUDA(cudaStreamSynchronize(h->stream));
+    }
     memcpy(x, h->h_x, bytes);
     return TPRGB_OK;
 }

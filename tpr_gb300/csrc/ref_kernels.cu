@@ -637,12 +637,16 @@ cr_tail(T *wa, T *wc, T *wr, long long wstride, T *gx, long long xstride,
 // Per row the operations and their order are those of fused_tpr.  gd (may
 // be null): the diagonal, dividing a, c, r on load exactly as the 4-argument
 // setter does (normalize_kernel) -- so inputs and output may also sit in
-// pinned host memory and one launch serves a whole host round trip.
+// pinned host memory and one launch serves a whole host round trip.  done
+// (may be null; a word the host reads): every CTA adds 1 once its part of
+// x is visible system-wide, so the host can watch a system complete
+// without a driver synchronisation.
 template <typename T, int KIND, int EPT>
 __global__ void __launch_bounds__(kThreads)
 cluster_tpr(const T *__restrict__ ga, const T *__restrict__ gd,
             const T *__restrict__ gc, const T *__restrict__ gr,
-            T *__restrict__ gx, int n, int s, long long stride) {
+            T *__restrict__ gx, int n, int s, long long stride,
+            unsigned *done) {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -763,6 +767,11 @@ cluster_tpr(const T *__restrict__ ga, const T *__restrict__ gd,
         }
     }
     for (int i = threadIdx.x; i < s; i += blockDim.x) gx[i] = x[i];
+    if (done) {  // count this CTA's slice as written, at system scope
+        __threadfence_system();
+        __syncthreads();
+        if (threadIdx.x == 0) atomicAdd_system(done, 1u);
+    }
 }
 
 // ---- sliced shape (large systems) ---------------------------------------
@@ -983,7 +992,7 @@ bool ref_needs_workspace(int kind, int n, int s, int prec) {
 template <typename T, int KIND, int EPT>
 static int launch_cluster_tpr(int nsys, int n, int s, const T *a, const T *diag,
                               const T *c, const T *r, T *x, long long stride,
-                              cudaStream_t st) {
+                              unsigned *done, cudaStream_t st) {
     const int m = n / s;
     const size_t smem = (7ULL * s + 10ULL * m + 3) * sizeof(T);
     const int threads = std::min(refk::kThreads, std::max(32, s));
@@ -1009,18 +1018,19 @@ static int launch_cluster_tpr(int nsys, int n, int s, const T *a, const T *diag,
     cfg.stream = st;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    TPRGB_CUDA(cudaLaunchKernelEx(&cfg, k, a, diag, c, r, x, n, s, stride));
+    TPRGB_CUDA(cudaLaunchKernelEx(&cfg, k, a, diag, c, r, x, n, s, stride, done));
     return TPRGB_OK;
 }
 
 template <typename T, int KIND>
 static int launch_cluster_ept(int nsys, int n, int s, const T *a, const T *diag, const T *c,
-                              const T *r, T *x, long long stride, cudaStream_t st) {
+                              const T *r, T *x, long long stride, unsigned *done,
+                              cudaStream_t st) {
     switch (std::max(1, s / refk::kThreads)) {
-        case 1: return launch_cluster_tpr<T, KIND, 1>(nsys, n, s, a, diag, c, r, x, stride, st);
-        case 2: return launch_cluster_tpr<T, KIND, 2>(nsys, n, s, a, diag, c, r, x, stride, st);
-        case 4: return launch_cluster_tpr<T, KIND, 4>(nsys, n, s, a, diag, c, r, x, stride, st);
-        default: return launch_cluster_tpr<T, KIND, 8>(nsys, n, s, a, diag, c, r, x, stride, st);
+        case 1: return launch_cluster_tpr<T, KIND, 1>(nsys, n, s, a, diag, c, r, x, stride, done, st);
+        case 2: return launch_cluster_tpr<T, KIND, 2>(nsys, n, s, a, diag, c, r, x, stride, done, st);
+        case 4: return launch_cluster_tpr<T, KIND, 4>(nsys, n, s, a, diag, c, r, x, stride, done, st);
+        default: return launch_cluster_tpr<T, KIND, 8>(nsys, n, s, a, diag, c, r, x, stride, done, st);
     }
 }
 
@@ -1031,7 +1041,7 @@ static int launch_tpr_kind(int nsys, int n, int s, const T *a, const T *c,
     const int m = n / s;
     if (ref_uses_fused<T>(KIND, n, s) && m >= 2 && m <= 16) {
         // one slice per CTA of a thread-block cluster
-        return launch_cluster_ept<T, KIND>(nsys, n, s, a, nullptr, c, r, x, stride, st);
+        return launch_cluster_ept<T, KIND>(nsys, n, s, a, nullptr, c, r, x, stride, nullptr, st);
     }
     if (ref_uses_fused<T>(KIND, n, s)) {
         size_t smem = (size_t)refk::fused_elems(n, s) * sizeof(T);
@@ -1193,7 +1203,8 @@ bool ref_direct_ok(int kind, int n, int s, int prec) {
 }
 
 int launch_ref_direct(int kind, int n, int s, int prec, const void *a, const void *diag,
-                      const void *c, const void *r, void *x, cudaStream_t st) {
+                      const void *c, const void *r, void *x, unsigned *done,
+                      cudaStream_t st) {
     if (!ref_direct_ok(kind, n, s, prec))
         return fail(TPRGB_EUNSUPPORTED, "no one-launch path for n=%d, s=%d", n, s);
     if (prec == TPRGB_F32) {
@@ -1201,7 +1212,7 @@ int launch_ref_direct(int kind, int n, int s, int prec, const void *a, const voi
             constexpr int K = decltype(kd)::value;
             return launch_cluster_ept<float, K>(1, n, s, (const float *)a, (const float *)diag,
                                                 (const float *)c, (const float *)r,
-                                                (float *)x, n, st);
+                                                (float *)x, n, done, st);
         };
         return kind == TPRGB_PTPR ? f(std::integral_constant<int, TPRGB_PTPR>())
                                   : f(std::integral_constant<int, TPRGB_TPR>());
@@ -1210,7 +1221,7 @@ int launch_ref_direct(int kind, int n, int s, int prec, const void *a, const voi
         constexpr int K = decltype(kd)::value;
         return launch_cluster_ept<double, K>(1, n, s, (const double *)a, (const double *)diag,
                                              (const double *)c, (const double *)r,
-                                             (double *)x, n, st);
+                                             (double *)x, n, done, st);
     };
     return kind == TPRGB_PTPR ? f(std::integral_constant<int, TPRGB_PTPR>())
                               : f(std::integral_constant<int, TPRGB_TPR>());
