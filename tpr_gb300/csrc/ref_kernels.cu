@@ -137,7 +137,11 @@ __device__ int ptpr_stage1_slice(T *a0, T *c0, T *r0, T *a1, T *c1, T *r1, int s
 template <typename T, int EPT>
 __device__ void tpr_stage1_slice(T *a, T *c, T *r, int s) {
     const int ls = ilog2(s);
-    for (int p = 1; p <= ls; p++) {
+    // levels from pw on update at most 32 rows (2 s / 2^p): warp 0 runs them
+    // alone with warp barriers; the caller's CTA barrier publishes them
+    int pw = ls + 1;
+    while (pw - 1 >= 2 && ((2 * s) >> (pw - 1)) <= 32) pw--;
+    for (int p = 1; p < pw; p++) {
         const int u = 1 << (p - 1), p2k = 1 << p;
         T na[EPT], nc[EPT], nr[EPT];
         bool sel[EPT];
@@ -165,6 +169,27 @@ __device__ void tpr_stage1_slice(T *a, T *c, T *r, int s) {
             }
         }
         __syncthreads();
+    }
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        for (int p = pw; p <= ls; p++) {  // lane: row pair k = lane / 2, end lane & 1
+            const int u = 1 << (p - 1), p2k = 1 << p;
+            const int k = lane >> 1;
+            if (k < (s >> p)) {
+                const int i = k * p2k + ((lane & 1) ? p2k - 1 : 0);
+                T na, nc, nr;
+                if (i == 0)
+                    upd_upper(a, c, r, i, i + u, na, nc, nr);
+                else if (i == s - 1)
+                    upd_lower(a, c, r, i - u, i, na, nc, nr);
+                else
+                    upd_mid(a, c, r, i - u, i, i + u, na, nc, nr);
+                a[i] = na;
+                c[i] = nc;
+                r[i] = nr;
+            }
+            __syncwarp();
+        }
     }
 }
 
@@ -360,6 +385,62 @@ __device__ void cta_cr(T *a, T *c, T *r, T *x, int m) {
             x[i] = cr_back_row<T>(a, c, r, x, i, u);
         }
         __syncthreads();
+    }
+}
+
+// PCR on m <= 32 rows by one warp (lane k: row k): cta_pcr's arithmetic and
+// order with warp barriers; the caller's CTA barrier publishes the result.
+template <typename T>
+__device__ void warp_pcr(T *a, T *c, T *r, int m) {
+    const int lane = threadIdx.x & 31;
+    const int pn = ilog2(m);
+    for (int p = 0; p < pn; p++) {
+        T na, nc, nr;
+        if (lane < m) pcr_row<T>(a, c, r, lane, m, 1 << p, na, nc, nr);
+        __syncwarp();
+        if (lane < m) {
+            a[lane] = na;
+            c[lane] = nc;
+            r[lane] = nr;
+        }
+        __syncwarp();
+    }
+}
+
+// CR on m <= 32 rows by one warp, solution into x: cta_cr's arithmetic and
+// order with warp barriers.
+template <typename T>
+__device__ void warp_cr(T *a, T *c, T *r, T *x, int m) {
+    const int lane = threadIdx.x & 31;
+    if (m <= 1) {
+        if (lane == 0) x[0] = r[0];
+        __syncwarp();
+        return;
+    }
+    const int ln = ilog2(m);
+    for (int p = 0; p < ln - 1; p++) {
+        const int u = 1 << p, ux = 2 * u;
+        const int i = ux - 1 + ux * lane;
+        const bool on = lane < m / ux;
+        T na, nc, nr;
+        if (on) cr_row<T>(a, c, r, i, u, m, na, nc, nr);
+        __syncwarp();
+        if (on) {
+            a[i] = na;
+            c[i] = nc;
+            r[i] = nr;
+        }
+        __syncwarp();
+    }
+    if (lane == 0) cr_top<T>(a, c, r, x, m);
+    __syncwarp();
+    for (int k = ln - 2; k >= 0; k--) {
+        const int u = 1 << k;
+        if (lane < m / (2 * u)) {
+            const int i = u - 1 + 2 * u * lane;
+            x[i] = cr_back_row<T>(a, c, r, x, i, u);
+        }
+        __syncwarp();
     }
 }
 
@@ -654,7 +735,8 @@ cluster_tpr(const T *__restrict__ ga, const T *__restrict__ gd,
     const int m = n / s;
     const int j = (int)cluster.block_rank();
     T *a = sm, *c = sm + s, *r = sm + 2 * s, *x = sm + 3 * s;
-    T *a2 = sm + 4 * s, *c2 = sm + 5 * s, *r2 = sm + 6 * s;  // PTPR's second copy
+    // PTPR's second copy; TPR keeps its loaded even rows there for stage 3
+    T *a2 = sm + 4 * s, *c2 = sm + 5 * s, *r2 = sm + 6 * s;
     T *ends = sm + 7 * s;  // [m][6]: E_st (a, c, r) after the update, E_ed (a, c, r)
     T *sa = ends + 6 * m, *sc = sa + m, *sr = sc + m, *sx = sr + m;
     T *bk = sx + m;        // this slice's E_st before the update (PTPR)
@@ -676,7 +758,14 @@ cluster_tpr(const T *__restrict__ ga, const T *__restrict__ gd,
             r[i] = gr[i];
         }
     };
-    for (int i = threadIdx.x; i < s; i += blockDim.x) load(i);
+    for (int i = threadIdx.x; i < s; i += blockDim.x) {
+        load(i);
+        if (KIND == TPRGB_TPR && (i & 1) == 0) {
+            a2[i] = a[i];
+            c2[i] = c[i];
+            r2[i] = r[i];
+        }
+    }
     // every CTA of the cluster must have started (its shared memory
     // exists) before any CTA writes into it: arrive now, wait just before
     // the writes, so the barrier's latency overlaps stage 1
@@ -712,22 +801,28 @@ cluster_tpr(const T *__restrict__ ga, const T *__restrict__ gd,
         dst[5] = r[s - 1];
     }
     cluster.sync();  // every slice's rows are in every CTA; no remote access after
-    for (int q = threadIdx.x; q < m; q += blockDim.x) {
-        const T *e = ends + 6 * q;
-        if (q < m - 1)  // E_ed of slice q with E_st of slice q + 1
-            inter_eq(e[3], e[4], e[5], e[6], e[7], e[8], sa[q], sc[q], sr[q]);
-        else {
-            sa[q] = e[3];
-            sc[q] = e[4];
-            sr[q] = e[5];
+    if (threadIdx.x < 32) {  // warp 0: the m <= 16 reduced equations and stage 2
+        for (int q = threadIdx.x; q < m; q += 32) {
+            const T *e = ends + 6 * q;
+            if (q < m - 1)  // E_ed of slice q with E_st of slice q + 1
+                inter_eq(e[3], e[4], e[5], e[6], e[7], e[8], sa[q], sc[q], sr[q]);
+            else {
+                sa[q] = e[3];
+                sc[q] = e[4];
+                sr[q] = e[5];
+            }
         }
+        __syncwarp();
+        if (KIND == TPRGB_PTPR)
+            warp_pcr<T>(sa, sc, sr, m);  // src/ptpr.cpp:246-258
+        else
+            warp_cr<T>(sa, sc, sr, sx, m);  // src/tpr.cpp:263-275
     }
     __syncthreads();
     // x of the previous slice's last row (0 before the first) and of this
     // slice's last row, from stage 2
     T xprev, xed;
     if (KIND == TPRGB_PTPR) {
-        cta_pcr<T, 1>(sa, sc, sr, m);  // src/ptpr.cpp:246-258 (m <= 16 rows)
         xprev = j > 0 ? sr[j - 1] : T(0);
         xed = sr[j];
         if (threadIdx.x == 0) {  // restore E_st, src/ptpr.cpp:266-271
@@ -745,17 +840,35 @@ cluster_tpr(const T *__restrict__ ga, const T *__restrict__ gd,
         if (threadIdx.x == 0) x[s - 1] = xed;
         __syncthreads();
     } else {
-        cta_cr<T, 1>(sa, sc, sr, sx, m);  // src/tpr.cpp:263-275 (m <= 16 rows)
         xprev = j > 0 ? sx[j - 1] : T(0);
         xed = sx[j];
-        // restore: even slice-local rows from the untouched inputs, odd
-        // rows keep their post-stage-1 values (src/tpr.cpp:236-325,381-387)
+        // restore: even slice-local rows as loaded, odd rows keep their
+        // post-stage-1 values (src/tpr.cpp:236-325,381-387)
         for (int i = threadIdx.x; i < s; i += blockDim.x)
-            if ((i & 1) == 0) load(i);
+            if ((i & 1) == 0) {
+                a[i] = a2[i];
+                c[i] = c2[i];
+                r[i] = r2[i];
+            }
         if (threadIdx.x == 0) x[s - 1] = xed;
         __syncthreads();
         const int ls = ilog2(s);
-        for (int p = ls - 1; p >= 0; p--) {  // src/tpr.cpp:277-308
+        // src/tpr.cpp:277-308; the levels of at most 32 rows on warp 0
+        int p = ls - 1;
+        while (p >= 0 && (s >> (p + 1)) <= 32) p--;
+        if (threadIdx.x < 32) {
+            for (int pp = ls - 1; pp > p; pp--) {
+                const int u = 1 << pp;
+                if (threadIdx.x < (s >> (pp + 1))) {
+                    const int i = u - 1 + 2 * u * (int)threadIdx.x;
+                    const T xu = i - u < 0 ? xprev : x[i - u];
+                    x[i] = r[i] - a[i] * xu - c[i] * x[i + u];
+                }
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        for (; p >= 0; p--) {
             const int u = 1 << p;
             const int per = s / (2 * u);
             for (int q = threadIdx.x; q < per; q += blockDim.x) {
