@@ -826,14 +826,25 @@ __device__ __forceinline__ bool run_tile_smem(
                 }
                 const float ea[4] = {ua.x, ua.y, ua.z, ua.w}, eb[4] = {ub.x, ub.y, ub.z, ub.w};
                 const float ec[4] = {uc.x, uc.y, uc.z, uc.w}, ed[4] = {ud.x, ud.y, ud.z, ud.w};
+                // the coefficients as doubles: bit-built on the integer
+                // pipes, or converted on the FP64 pipe for a unit holding a
+                // value that is not a normal float or zero
+                bool odd = false;
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+                    odd = odd || hier::f32_odd(ea[j]) || hier::f32_odd(eb[j]) ||
+                          hier::f32_odd(ec[j]) || hier::f32_odd(ed[j]);
+                auto cv = [odd](float f) {
+                    return odd ? (double)f : hier::f32_to_f64_bits(f);
+                };
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
                     const int i = 4 * u + j;
                     const float ai = (i == 0 && first_eq) ? 0.f : ea[j];
                     const float ci = (i == L - 1 && last_eq) ? 0.f : ec[j];
-                    double rr = fma(-(double)eb[j], xd[i], (double)ed[j]);
-                    rr = fma(-(double)ai, i > 0 ? xd[i - 1] : xm, rr);
-                    rr = fma(-(double)ci, i < L - 1 ? xd[i + 1] : xp, rr);
+                    double rr = fma(-cv(eb[j]), xd[i], cv(ed[j]));
+                    rr = fma(-cv(ai), i > 0 ? xd[i - 1] : xm, rr);
+                    rr = fma(-cv(ci), i < L - 1 ? xd[i + 1] : xp, rr);
                     r[i] = (float)rr;
                 }
             }
@@ -844,8 +855,16 @@ __device__ __forceinline__ bool run_tile_smem(
                 if (step == refine_steps - 1) stage_free();
                 solve<L, NT, T, PP>(a, b, c, r, dx, sm, pc);
             }
+            bool odd = false;
 #pragma unroll
-            for (int i = 0; i < L; i++) xd[i] += (double)dx[i];
+            for (int i = 0; i < L; i++) odd = odd || hier::f32_odd(dx[i]);
+            if (odd) {
+#pragma unroll
+                for (int i = 0; i < L; i++) xd[i] += (double)dx[i];
+            } else {
+#pragma unroll
+                for (int i = 0; i < L; i++) xd[i] += hier::f32_to_f64_bits(dx[i]);
+            }
         }
         if (!active) return true;
         bool finite = true;
