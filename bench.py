@@ -21,6 +21,11 @@ from its sources where present (oracle/_ref), else the C restatement (oracle
 port, same bits).  The in-arm cpu_baseline times the same 2048-system
 samples for --cpu-seconds; plain_single_system adds the N=2048, S=512 single
 solve on the GPU beside the reference's CPU PTPR / TPR on the host cores.
+At N=1, after the timed region, `rows` adds the other configurations the
+reference's benchmark names, measured on this GPU: the uneven batch (4096
+systems of 2^U{6..16} through a plan), the precision stress (1024 x 32768,
+weakly dominant) and serving (Poisson arrivals, 20000 requests per load);
+--no-rows leaves them out.
 """
 from __future__ import annotations
 
@@ -223,6 +228,23 @@ def plain_row(iters=1000):
     gpu.pop("workload", None)
     return {"workload": "one system N=2048, S=512, FP32, seed 42, "
                         f"{iters} solves", "gpu": gpu, "cpu_reference": cpu}
+
+
+def other_rows():
+    """The uneven-batch, precision-stress and serving configurations,
+    measured after the bench's timed region (compact fields; the full
+    records come from python -m tpr_gb300.workloads / serve_bench)."""
+    from tpr_gb300 import serve_bench as SB
+    from tpr_gb300 import workloads as W
+    un = W.uneven()
+    un.pop("plan", None)
+    pr = W.precision()
+    sv = SB.run(20000)
+    serving = {"workload": sv["workload"], "saturated": sv["saturated"],
+               "loads": [{k: ld[k] for k in ("load", "p50_ms", "p99_ms",
+                                             "p99_over_p50", "systems_per_s", "rc")}
+                         for ld in sv["loads"]]}
+    return {"uneven": un, "precision": pr, "serving": serving}
 
 
 def run_reference(args):
@@ -430,6 +452,8 @@ def run_ours(args):
             line["cpu_baseline"] = cpu
         if plain:
             line["plain_single_system"] = plain
+        if world == 1 and not args.no_rows:
+            line["rows"] = other_rows()
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -444,6 +468,8 @@ def main():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-rows", action="store_true",
+                   help="leave out the uneven / precision / serving rows")
     args = p.parse_args()
     if args.impl == "reference":
         return run_reference(args)
