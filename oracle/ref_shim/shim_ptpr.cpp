@@ -3,7 +3,7 @@
 // (PCR_SINGLE_THREAD, as src/CMakeLists.txt:69-75 builds them).
 // TEST INFRASTRUCTURE ONLY: the result of this file is oracle/_ref/, the
 // reference itself, used to pin the oracle restatement and as the
-// reference-kind CPU baseline in this container.
+// reference-kind CPU baseline wherever the reference tree is present.
 #include <omp.h>
 
 #include <cstring>
