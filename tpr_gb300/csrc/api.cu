@@ -92,6 +92,11 @@ struct tprgb_solver {
     // counts enqueued and confirmed) instead of a driver synchronisation.
     unsigned *h_done = nullptr, *hd_done = nullptr;
     unsigned expect = 0, seen = 0;
+    // The one-launch solve as a CUDA graph (its arguments never change: the
+    // staging, the completion word; [1] with the diagonal), captured at the
+    // second solve and replayed after; graph_failed: launch directly.
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    bool graph_failed = false;
 };
 
 // Waits until every enqueued one-launch solve has written x (and so has
@@ -186,6 +191,8 @@ TPRGB_API int tprgb_normalize_device(int prec, int64_t neq, void *d_a,
 
 static void free_handle(tprgb_solver *h) {
     if (!h) return;
+    for (cudaGraphExec_t g : h->gexec)
+        if (g) cudaGraphExecDestroy(g);
     if (h->staged) cudaEventDestroy(h->staged);
     cudaFreeHost(h->h_stage);
     if (h->h_done) cudaFreeHost(h->h_done);
@@ -315,11 +322,39 @@ TPRGB_API int tprgb_solve(tprgb_solver *h, int *flops) {
     int rc;
     if (h->direct) {
         const size_t bytes = (size_t)h->n * h->esz;
-        rc = launch_ref_direct(h->kind, h->n, h->s, h->prec, h->hd_stage,
-                               h->use_diag ? h->hd_stage + 3 * bytes : nullptr,
-                               h->hd_stage + bytes, h->hd_stage + 2 * bytes,
-                               h->hd_stage + 4 * bytes, h->hd_done, h->stream);
-        if (rc) return rc;
+        auto launch = [&]() {
+            return launch_ref_direct(h->kind, h->n, h->s, h->prec, h->hd_stage,
+                                     h->use_diag ? h->hd_stage + 3 * bytes : nullptr,
+                                     h->hd_stage + bytes, h->hd_stage + 2 * bytes,
+                                     h->hd_stage + 4 * bytes, h->hd_done, h->stream);
+        };
+        cudaGraphExec_t &gx = h->gexec[h->use_diag ? 1 : 0];
+        // the first solve launches directly (and sets the kernel's
+        // attributes); later ones capture it once and replay the graph
+        if (!gx && !h->graph_failed && h->expect != 0) {
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                rc = launch();
+                cudaError_t ee = cudaStreamEndCapture(h->stream, &g);
+                if (rc == TPRGB_OK && ee == cudaSuccess)
+                    e = cudaGraphInstantiate(&gx, g, 0);
+                else
+                    e = ee != cudaSuccess ? ee : cudaErrorUnknown;
+                if (g) cudaGraphDestroy(g);
+            }
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                gx = nullptr;
+                h->graph_failed = true;
+            }
+        }
+        if (gx) {
+            TPRGB_CUDA(cudaGraphLaunch(gx, h->stream));
+        } else {
+            rc = launch();
+            if (rc) return rc;
+        }
         // the next set_system / get_ans waits for this solve's parts
         h->expect += (unsigned)(h->n / h->s);
     } else {
