@@ -220,6 +220,35 @@ def test_edge_shapes_vs_port(cuda, port, prec, kind):
 
 
 @pytest.mark.parametrize("prec", ["f32", "f64"])
+@pytest.mark.parametrize("cls,kind", [("PTPR", 0), ("TPR", 1)])
+def test_handle_repeated_solves(cuda, port, prec, cls, kind):
+    """One handle, many solves: the one-launch path is captured into a CUDA
+    graph at the second solve (one graph per setter form) and replayed,
+    and completion is read from the mapped word the kernel counts up.
+    New systems every time, the 3- and 4-argument setters alternating, a
+    solve whose x is never read before the next set: every x the same bits
+    as the C restatement."""
+    dt = np.float32 if prec == "f32" else np.float64
+    n, s = 2048, 512
+    t = getattr(T, cls)(n, s, dtype=dt)
+    ref = port.ptpr if kind == 0 else port.tpr
+    for it in range(7):
+        a, b, c, d, _ = G.one_system(n, 900 + it, "uneven")
+        a, b, c, d = (v.astype(dt) for v in (a, b, c, d))
+        if it % 2:
+            t.set_tridiagonal_system(a, b, c, d)
+        else:
+            t.set_tridiagonal_system(a / b, c / b, d / b)
+        t.solve()
+        if it == 3:
+            continue  # the next set waits for this solve
+        an, cn, rn = port.normalize(a, b, c, d, dt)
+        if it % 2 == 0:
+            an, cn, rn = a / b, c / b, d / b
+        _bits_equal(t.get_ans(), ref(an, cn, rn, s, dt)[0])
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
 def test_tiny_cr_pcr_vs_port(cuda, port, prec):
     """Standalone CR / PCR on n = 1, 2, 4, 8 (n = 1: x = rhs, no reduction;
     n = 2: the two-row solve alone): same bits as the C restatement."""
