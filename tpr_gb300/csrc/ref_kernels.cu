@@ -712,10 +712,12 @@ cr_tail(T *wa, T *wc, T *wr, long long wstride, T *gx, long long xstride,
 // j holding slice j: stage 1 of the m slices runs on m SMs at once.  After
 // the E_st update each CTA writes its slice's first row (E_st, updated) and
 // last row (E_ed) into every CTA's shared memory (distributed shared
-// memory, one cluster barrier); every CTA then forms the m reduced
-// equations and solves stage 2 itself -- the same arithmetic on the same
-// values, so the same bits in every CTA -- and runs stage 3 on its slice.
-// Per row the operations and their order are those of fused_tpr.  gd (may
+// memory, one cluster barrier); warp 0 of every CTA then forms the m
+// reduced equations and solves stage 2 itself -- the same arithmetic on the
+// same values, so the same bits in every CTA -- and the CTA runs stage 3 on
+// its slice.  Per row the operations and their order are those of
+// fused_tpr; steps touching at most 32 rows (the reduced system, TPR's top
+// tree and back-substitution levels) run on one warp with warp barriers.  gd (may
 // be null): the diagonal, dividing a, c, r on load exactly as the 4-argument
 // setter does (normalize_kernel) -- so inputs and output may also sit in
 // pinned host memory and one launch serves a whole host round trip.  done
