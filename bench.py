@@ -148,12 +148,15 @@ def profiled_traffic():
     if not os.path.exists(PROFILE):
         return None
     got = {}
-    unit = {"byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9}
+    unit = {"byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9,
+            "B": 1.0, "KB": 1e3, "MB": 1e6, "GB": 1e9}
     for line in open(PROFILE):
         for key in ("DRAM read", "DRAM write"):
             if line.startswith(f"| {key} |"):
                 v, u = line.split("|")[2].split()
-                got[key] = float(v) * unit.get(u, 1.0)
+                if u not in unit:
+                    return None
+                got[key] = float(v) * unit[u]
     if len(got) != 2:
         return None
     return got["DRAM read"] + got["DRAM write"]
